@@ -1,0 +1,336 @@
+"""accelerate-llvm_gb300 -- host-side mirror of Accelerate's PTX skeleton ops.
+
+Thin Python layer over ``libaccgb.so`` (the C ABI declared in
+``include/acc_gb300.h``).  Each function mirrors one `Execute PTX` skeleton op
+of accelerate-llvm-ptx (accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/
+PTX/Execute.hs:83-109) with the Accelerate names and argument meaning:
+
+    fold f z xs, fold1 f xs, fold_seg f z xs seg, fold1_seg f xs seg,
+    scanl/scanl1/scanr/scanr1, scanl_ (scanl'), scanr_ (scanr'),
+    permute f defaults idx xs, stencil (weighted sum) and stencil2.
+
+Arrays are CUDA tensors (torch is the device allocator and stream provider
+only); results are allocated here, as the reference allocates them with
+``allocateRemote``.  The combine function is one of the fixed primitives
+``'+' '*' 'min' 'max' 'and' 'or' 'xor'``; anything else raises, as the
+reference's shim raises ``internalError "unsupported combine function"``.
+
+There is no CPU fallback: importing this module on a machine where the
+library cannot be loaded raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+from typing import Optional, Sequence, Union
+
+import torch
+
+_HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libaccgb.so"
+
+# ----------------------------------------------------------------- enums (acc_gb300.h)
+I32, I64, U32, F32, F64 = range(5)
+ADD, MUL, MIN, MAX, AND, OR, XOR = range(7)
+PREC_DEFAULT, PREC_PLAIN, PREC_COMPENSATED, PREC_FP64ACC = range(4)
+L2R, R2L = 0, 1
+SCAN_INCLUSIVE, SCAN_SEEDED, SCAN_PRIME = range(3)
+CLAMP, MIRROR, WRAP, CONSTANT = range(4)
+
+OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "UNSUPPORTED", 3: "EMPTY", 4: "CUDA", 5: "NOMEM",
+                6: "TIMEOUT", 7: "INDEX", 8: "TOO_LARGE"}
+
+OPS = {"+": ADD, "add": ADD, "*": MUL, "mul": MUL, "min": MIN, "max": MAX,
+       "and": AND, ".&.": AND, "or": OR, ".|.": OR, "xor": XOR}
+BOUNDARIES = {"clamp": CLAMP, "mirror": MIRROR, "wrap": WRAP, "constant": CONSTANT}
+PRECS = {None: PREC_DEFAULT, "default": PREC_DEFAULT, "plain": PREC_PLAIN,
+         "compensated": PREC_COMPENSATED, "fp64": PREC_FP64ACC}
+
+_DTYPES = {torch.int32: I32, torch.int64: I64, torch.float32: F32, torch.float64: F64}
+if hasattr(torch, "uint32"):
+    _DTYPES[torch.uint32] = U32
+_CTYPES = {I32: ctypes.c_int32, I64: ctypes.c_int64, U32: ctypes.c_uint32, F32: ctypes.c_float,
+           F64: ctypes.c_double}
+
+
+class AccError(RuntimeError):
+    """A non-zero acc_status from the library."""
+
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        text = _lib.acc_strerror(status).decode() if _lib is not None else STATUS_NAMES.get(status, "?")
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)} ({text})" if what else text)
+
+
+# ----------------------------------------------------------------- loading
+_lib: Optional[ctypes.CDLL] = None
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_L = ctypes.c_int64
+SIGNATURES = {
+    "acc_version": ([], _I),
+    "acc_strerror": ([_I], ctypes.c_char_p),
+    "acc_sync": ([_P], _I),
+    "acc_release_workspaces": ([], _I),
+    "acc_fold": ([_I, _I, _I, _P, _P, _L, _L, _P, _P], _I),
+    "acc_fold_seg": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
+    "acc_fold_seg_lengths": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
+    "acc_scan": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
+    "acc_permute": ([_I, _I, _P, _P, _P, _I, _P, _L, _L, _P], _I),
+    "acc_permute_clone": ([_I, _I, _P, _P, _P, _P, _I, _P, _L, _L, _P], _I),
+    "acc_stencil2d": ([_I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _P], _I),
+    "acc_stencil2d_pair": ([_I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _L, _L, _P, _L, _L, _P, _P], _I),
+}
+
+
+def load(path: Union[str, pathlib.Path, None] = None) -> ctypes.CDLL:
+    """Load libaccgb.so (building it first if it is missing and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = pathlib.Path(path) if path else LIB_PATH
+    if not p.exists():
+        from . import build as _build  # noqa: F401  (only when imported as a package)
+        _build.build()
+    lib = ctypes.CDLL(str(p))
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def lib() -> ctypes.CDLL:
+    return _lib if _lib is not None else load()
+
+
+def _check(status: int, what: str) -> None:
+    if status != OK:
+        raise AccError(status, what)
+
+
+# ----------------------------------------------------------------- helpers
+def type_of(t: torch.Tensor) -> int:
+    try:
+        return _DTYPES[t.dtype]
+    except KeyError:
+        raise TypeError(f"unsupported element type {t.dtype}") from None
+
+
+def op_of(f) -> int:
+    if isinstance(f, int):
+        return f
+    try:
+        return OPS[f]
+    except KeyError:
+        raise ValueError(f"unsupported combine function {f!r} (fixed primitives only)") from None
+
+
+def _stream(stream=None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _seed_ptr(type_code: int, value):
+    if value is None:
+        return None, None
+    c = _CTYPES[type_code](value)
+    return ctypes.cast(ctypes.pointer(c), ctypes.c_void_p), c
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return ctypes.c_void_p(t.data_ptr() if t is not None else 0)
+
+
+def _dev(t: torch.Tensor) -> torch.Tensor:
+    if not t.is_cuda:
+        raise ValueError("arrays must be CUDA tensors")
+    return t.contiguous()
+
+
+def sync(stream=None) -> None:
+    """Wait for the stream and raise any device-side error (acc_sync)."""
+    _check(lib().acc_sync(_stream(stream)), "acc_sync")
+
+
+# ----------------------------------------------------------------- fold
+def fold(f, z, xs: torch.Tensor, prec=None, stream=None) -> torch.Tensor:
+    """fold f z xs: reduce the innermost dimension from the seed z (PTX/Execute.hs:237-249)."""
+    return _fold(f, z, xs, prec, stream)
+
+
+def fold1(f, xs: torch.Tensor, prec=None, stream=None) -> torch.Tensor:
+    """fold1 f xs: reduce the (non-empty) innermost dimension (PTX/Execute.hs:222-235)."""
+    return _fold(f, None, xs, prec, stream)
+
+
+def _fold(f, z, xs, prec, stream):
+    xs = _dev(xs)
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1] if shape else 1
+    outer_shape = shape[:-1]
+    outer = 1
+    for d in outer_shape:
+        outer *= d
+    out = torch.empty(outer_shape, dtype=xs.dtype, device=xs.device)
+    sp, _keep = _seed_ptr(tc, z)
+    st = lib().acc_fold(op_of(f), tc, PRECS[prec], _ptr(xs), _ptr(out), outer, inner, sp, _stream(stream))
+    _check(st, "fold")
+    return out
+
+
+# ----------------------------------------------------------------- foldSeg
+def fold_seg(f, z, xs: torch.Tensor, seg: torch.Tensor, prec=None, stream=None, offsets: bool = True):
+    """foldSeg f z xs seg.  `seg` holds nseg+1 offsets (the reference's input after
+    `scanl (+) 0`, PTX/Execute.hs:359) or, with offsets=False, nseg lengths."""
+    return _fold_seg(f, z, xs, seg, prec, stream, offsets)
+
+
+def fold1_seg(f, xs: torch.Tensor, seg: torch.Tensor, prec=None, stream=None, offsets: bool = True):
+    return _fold_seg(f, None, xs, seg, prec, stream, offsets)
+
+
+def _fold_seg(f, z, xs, seg, prec, stream, offsets):
+    xs = _dev(xs)
+    seg = _dev(seg)
+    tc = type_of(xs)
+    st_ = type_of(seg)
+    shape = tuple(xs.shape)
+    inner = shape[-1]
+    outer = 1
+    for d in shape[:-1]:
+        outer *= d
+    nseg = seg.numel() - 1 if offsets else seg.numel()
+    out = torch.empty(shape[:-1] + (nseg,), dtype=xs.dtype, device=xs.device)
+    sp, _keep = _seed_ptr(tc, z)
+    fn = lib().acc_fold_seg if offsets else lib().acc_fold_seg_lengths
+    _check(fn(op_of(f), tc, PRECS[prec], _ptr(xs), _ptr(seg), st_, _ptr(out), outer, inner, nseg, sp,
+              _stream(stream)), "foldSeg")
+    return out
+
+
+# ----------------------------------------------------------------- scans
+def _scan(f, z, xs, direction, kind, prec, stream):
+    xs = _dev(xs)
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1]
+    outer = 1
+    for d in shape[:-1]:
+        outer *= d
+    out_inner = inner + 1 if kind == SCAN_SEEDED else inner
+    out = torch.empty(shape[:-1] + (out_inner,), dtype=xs.dtype, device=xs.device)
+    sums = torch.empty(shape[:-1], dtype=xs.dtype, device=xs.device) if kind == SCAN_PRIME else None
+    sp, _keep = _seed_ptr(tc, z)
+    st = lib().acc_scan(op_of(f), tc, PRECS[prec], direction, kind, _ptr(xs), _ptr(out),
+                        _ptr(sums) if sums is not None else None, outer, inner, sp, _stream(stream))
+    _check(st, "scan")
+    return (out, sums) if kind == SCAN_PRIME else out
+
+
+def scanl(f, z, xs, prec=None, stream=None):
+    """scanl f z xs (output one longer, z first; PTX/Execute.hs:377-389)."""
+    return _scan(f, z, xs, L2R, SCAN_SEEDED, prec, stream)
+
+
+def scanl1(f, xs, prec=None, stream=None):
+    return _scan(f, None, xs, L2R, SCAN_INCLUSIVE, prec, stream)
+
+
+def scanr(f, z, xs, prec=None, stream=None):
+    return _scan(f, z, xs, R2L, SCAN_SEEDED, prec, stream)
+
+
+def scanr1(f, xs, prec=None, stream=None):
+    return _scan(f, None, xs, R2L, SCAN_INCLUSIVE, prec, stream)
+
+
+def scanl_(f, z, xs, prec=None, stream=None):
+    """scanl' f z xs -> (exclusive scan, totals) (PTX/Execute.hs:491-512)."""
+    return _scan(f, z, xs, L2R, SCAN_PRIME, prec, stream)
+
+
+def scanr_(f, z, xs, prec=None, stream=None):
+    return _scan(f, z, xs, R2L, SCAN_PRIME, prec, stream)
+
+
+# ----------------------------------------------------------------- permute
+def permute(f, defaults: torch.Tensor, idx: torch.Tensor, xs: Union[torch.Tensor, int, float, None] = None,
+            n: Optional[int] = None, stream=None) -> torch.Tensor:
+    """permute f defaults p xs with p given as a target-index array (negative =
+    Nothing).  `xs` is a source array, or a scalar for a constant (fused fill)
+    source of length n (default: len(idx))."""
+    defaults = _dev(defaults)
+    idx = _dev(idx)
+    tc = type_of(defaults)
+    it = type_of(idx)
+    out = torch.empty_like(defaults)
+    n_ = idx.numel() if n is None else n
+    if isinstance(xs, torch.Tensor):
+        xs = _dev(xs)
+        if xs.dtype != defaults.dtype:
+            raise TypeError("source and target element types differ")
+        srcp, cvp, keep = _ptr(xs), None, None
+    else:
+        cvp, keep = _seed_ptr(tc, 1 if xs is None else xs)
+        srcp = None
+    st = lib().acc_permute_clone(op_of(f), tc, _ptr(defaults), srcp, cvp, _ptr(idx), it, _ptr(out), n_,
+                                 defaults.numel(), _stream(stream))
+    _check(st, "permute")
+    return out
+
+
+# ----------------------------------------------------------------- stencil
+def stencil(weights: Sequence[Sequence[float]], xs: torch.Tensor, boundary="clamp", cval=None,
+            stream=None) -> torch.Tensor:
+    """stencil over a rank-1 or rank-2 array with a weighted-sum stencil
+    function; weights is a (2ry+1) x (2rx+1) nested list (rank-1: one row)."""
+    xs = _dev(xs)
+    tc = type_of(xs)
+    rows = [list(r) for r in weights]
+    ky, kx = len(rows), len(rows[0])
+    if ky % 2 == 0 or kx % 2 == 0 or any(len(r) != kx for r in rows):
+        raise ValueError("stencil pattern must be odd-sized and rectangular")
+    flat = [v for r in rows for v in r]
+    warr = (_CTYPES[tc] * len(flat))(*flat)
+    h, w = (1, xs.shape[0]) if xs.dim() == 1 else tuple(xs.shape)
+    out = torch.empty_like(xs)
+    b = BOUNDARIES[boundary] if isinstance(boundary, str) else boundary
+    cvp, keep = _seed_ptr(tc, cval if cval is not None else 0)
+    st = lib().acc_stencil2d(tc, ky // 2, kx // 2, ctypes.cast(warr, ctypes.c_void_p), b, cvp, _ptr(xs),
+                             _ptr(out), h, w, _stream(stream))
+    _check(st, "stencil")
+    return out
+
+
+def stencil2(wa, wb, a: torch.Tensor, b: torch.Tensor, boundary_a="clamp", boundary_b="clamp", cval_a=None,
+             cval_b=None, stream=None) -> torch.Tensor:
+    """stencil2: weighted sums of two arrays' neighbourhoods over the
+    intersection of their shapes (PTX/Execute.hs:669-684)."""
+    a = _dev(a)
+    b = _dev(b)
+    tc = type_of(a)
+    if type_of(b) != tc:
+        raise TypeError("stencil2 inputs must share an element type here")
+    ra, rb = [list(r) for r in wa], [list(r) for r in wb]
+    ky, kx = len(ra), len(ra[0])
+    if (len(rb), len(rb[0])) != (ky, kx):
+        raise ValueError("both stencil patterns must have the same size")
+    fa = (_CTYPES[tc] * (ky * kx))(*[v for r in ra for v in r])
+    fb = (_CTYPES[tc] * (ky * kx))(*[v for r in rb for v in r])
+    (ha, wa), (hb, wb) = [(1, t.shape[0]) if t.dim() == 1 else tuple(t.shape) for t in (a, b)]
+    h, w = min(ha, hb), min(wa, wb)
+    out = torch.empty((h, w) if a.dim() == 2 else (w,), dtype=a.dtype, device=a.device)
+    ba = BOUNDARIES[boundary_a] if isinstance(boundary_a, str) else boundary_a
+    bb = BOUNDARIES[boundary_b] if isinstance(boundary_b, str) else boundary_b
+    ca, ka = _seed_ptr(tc, cval_a if cval_a is not None else 0)
+    cb, kb = _seed_ptr(tc, cval_b if cval_b is not None else 0)
+    st = lib().acc_stencil2d_pair(tc, ky // 2, kx // 2, ctypes.cast(fa, ctypes.c_void_p),
+                                  ctypes.cast(fb, ctypes.c_void_p), ba, ca, bb, cb, _ptr(a), ha, wa, _ptr(b), hb, wb,
+                                  _ptr(out), _stream(stream))
+    _check(st, "stencil2")
+    return out

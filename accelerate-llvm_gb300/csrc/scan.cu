@@ -1,0 +1,550 @@
+// scan.cu -- scanl / scanl1 / scanr / scanr1 / scanl' / scanr' for the fixed
+// primitives.
+//
+// The reference runs a 1-D scan as three kernels (scanP1 block scans, a
+// single-block scanP2 over the block totals, scanP3 adding the carries:
+// accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/PTX/Execute.hs:422-468,
+// PTX/CodeGen/Scan.hs:141-439), about 4n words of traffic.  Here a 1-D scan is
+// ONE pass of 2n words: a single-pass scan with decoupled look-back
+// (Merrill & Garland 2016).  Each CTA
+//   1. takes a tile index from an atomic ticket (tiles are handed out in
+//      order, so every tile it may wait on belongs to a CTA that is running),
+//   2. pulls its 32 KiB tile into shared memory with one 2-D TMA load of a
+//      [rows x 128 B] view of the array, 128-byte swizzled so that the
+//      thread-per-row reads below are bank-conflict free,
+//   3. reduces each thread's 128-byte row serially, scans the thread totals
+//      with warp shuffles, publishes the tile aggregate, and (warp 0) looks
+//      back over the predecessors' published aggregates / inclusive prefixes,
+//   4. rescans its row from the tile prefix and writes the result back to the
+//      same swizzled smem buffer, from which one TMA store writes the tile.
+// Element semantics follow accelerate-llvm-native/src/Data/Array/Accelerate/
+// LLVM/Native/CodeGen/Scan.hs:136-270: left-to-right combines `f acc x`,
+// right-to-left `f x acc`; the seed sits at the far left (L2R) or far right
+// (R2L).  The primitives are commutative, so one push() serves both.
+//
+// Rows of a rank >= 2 array are scanned by scan_rows_kernel: one CTA per row
+// with a carried prefix, as the reference's `scan` (multi-dim) kernel does
+// (PTX/CodeGen/Scan.hs:746-939).
+#include "common.cuh"
+
+namespace accgb {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ROW_BYTES = 128;  // one thread row = one 128 B swizzle line
+
+struct ScanArgs {
+  const void *in;
+  void *out;
+  void *total_out;   // grand total (scanl z -> out+n, scan' -> sums) or null
+  void *seed_out;    // where to store the seed (scanr z -> out+n) or null
+  int64_t n;
+  int64_t full_rows;  // rows of 128 B fully inside the array
+  int64_t ntiles;
+  uint64_t seed;      // seed bits
+  uint64_t *status;
+  uint32_t *ticket;
+  uint32_t *err;
+  uint32_t epoch;
+  int has_seed;
+  int exclusive;
+  int tma_in;
+  int tma_out;
+};
+
+__device__ __forceinline__ int swz(int row, int chunk) { return row * SCAN_ROW_BYTES + ((chunk ^ (row & 7)) << 4); }
+
+// Publish a look-back status of tile t: (flag, value), flag 1 = aggregate,
+// 2 = inclusive prefix.  Each 64-bit slot word carries the 32-bit tag
+// (epoch << 2 | flag) next to 32 bits of the value, so every word is
+// self-describing; an 8-byte value uses two words that a reader accepts only
+// when both carry the same tag.
+template <class S>
+__device__ __forceinline__ void publish(uint64_t *status, int64_t t, uint32_t epoch, uint32_t flag, S v) {
+  uint64_t b = to_bits(v);
+  uint64_t tag = (uint64_t)((epoch << 2) | flag) << 32;
+  if constexpr (sizeof(S) == 8) st_relaxed_u64(status + 2 * t + 1, tag | (b >> 32));
+  st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
+}
+
+// Read the status of tile t; returns the flag (0 = not yet published).
+template <class S>
+__device__ __forceinline__ uint32_t peek(const uint64_t *status, int64_t t, uint32_t epoch, S &v) {
+  uint64_t w0 = ld_relaxed_u64(status + 2 * t);
+  uint32_t tag = (uint32_t)(w0 >> 32);
+  if ((tag >> 2) != epoch) return 0;
+  uint64_t b = w0 & 0xffffffffull;
+  if constexpr (sizeof(S) == 8) {
+    uint64_t w1 = ld_relaxed_u64(status + 2 * t + 1);
+    if ((uint32_t)(w1 >> 32) != tag) return 0;
+    b |= (w1 & 0xffffffffull) << 32;
+  }
+  v = from_bits<S>(b);
+  return tag & 3u;
+}
+
+template <int OP, class T, int PREC, bool R2L>
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_lookback_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int TILE = SCAN_THREADS * ITEMS;
+  constexpr int NWARP = SCAN_THREADS / 32;
+
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t bar;
+  __shared__ int64_t s_tile;
+  __shared__ S s_warp[NWARP];
+  __shared__ S s_prefix;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  if (tid == 0) {
+    uint32_t dyn = atomicAdd(a.ticket, 1u);
+    // The holder of the last ticket knows every other CTA has taken its
+    // ticket: it re-arms the counter for the next launch on this stream.
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    s_tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
+    if (a.tma_in) {
+      mbar_init(&bar, 1);
+      fence_mbar_init();
+    }
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t row0 = tile * SCAN_THREADS;  // first 128 B row of the tile
+  const T idT = Prim<OP, T>::id();
+
+  // ---------------------------------------------------------------- load
+  if (a.tma_in) {
+    if (tid == 0) {
+      prefetch_tmap(&tin);
+      mbar_expect_tx(&bar, TILE * sizeof(T));
+      tma_load_2d(buf, &tin, 0, (int)row0, &bar);
+    }
+    if (!mbar_wait(&bar, 0)) {
+      raise_error(a.err, DEV_ERR_TIMEOUT);
+      mbar_wait(&bar, 0);  // the copy is ours: give it a second bounded chance to land
+    }
+  } else {
+    // Coalesced loads into the same swizzled layout the TMA would produce.
+    const T *src = static_cast<const T *>(a.in);
+    const int64_t base = tile * (int64_t)TILE;
+    for (int e = tid; e < TILE; e += SCAN_THREADS) {
+      int64_t gi = base + e;
+      T v = gi < a.n ? src[gi] : idT;
+      int r = e / ITEMS, k = e % ITEMS;
+      *reinterpret_cast<T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T)) = v;
+    }
+    __syncthreads();
+  }
+
+  const int64_t myrow = row0 + tid;
+  const int64_t e0 = myrow * ITEMS;
+  T x[ITEMS];
+  const bool from_smem = !a.tma_in || myrow < a.full_rows;
+  if (from_smem) {
+#pragma unroll
+    for (int c = 0; c < ITEMS / VEC; ++c) {
+      uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(tid, c));
+      memcpy(&x[c * VEC], &v, 16);
+    }
+  } else {
+    const T *src = static_cast<const T *>(a.in);
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
+  }
+
+  // ---------------------------------------------------------------- reduce
+  S agg;
+  if (!R2L) {
+    agg = A::lift(x[0]);
+#pragma unroll
+    for (int j = 1; j < ITEMS; ++j) agg = A::push(agg, x[j]);
+  } else {
+    agg = A::lift(x[ITEMS - 1]);
+#pragma unroll
+    for (int j = ITEMS - 2; j >= 0; --j) agg = A::push(agg, x[j]);
+  }
+
+  S incl, excl_lane;
+  if (!R2L) {
+    incl = warp_scan_incl<A>(agg);
+    S up = shfl_up(incl, 1);
+    excl_lane = lane == 0 ? A::id() : up;
+    if (lane == 31) s_warp[warp] = incl;
+  } else {
+    incl = warp_scan_incl_rev<A>(agg);
+    S dn = shfl_down(incl, 1);
+    excl_lane = lane == 31 ? A::id() : dn;
+    if (lane == 0) s_warp[warp] = incl;
+  }
+  __syncthreads();
+
+  S wpre = A::id();
+  if (!R2L) {
+    for (int w = 0; w < warp; ++w) wpre = A::comb(wpre, s_warp[w]);
+  } else {
+    for (int w = warp + 1; w < NWARP; ++w) wpre = A::comb(wpre, s_warp[w]);
+  }
+
+  // ---------------------------------------------------------------- look-back
+  if (warp == 0) {
+    S bagg = s_warp[0];
+#pragma unroll
+    for (int w = 1; w < NWARP; ++w) bagg = A::comb(bagg, s_warp[w]);
+    const bool first = R2L ? (tile == a.ntiles - 1) : (tile == 0);
+    S prefix;
+    if (first) {
+      prefix = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
+    } else {
+      if (lane == 0) publish<S>(a.status, tile, a.epoch, 1u, bagg);
+      S acc = A::id();
+      int64_t k0 = 0;
+      bool gave_up = false;
+      while (true) {
+        const int64_t pt = R2L ? tile + 1 + k0 + lane : tile - 1 - k0 - lane;
+        const bool exists = R2L ? (pt < a.ntiles) : (pt >= 0);
+        uint32_t flag = exists ? 0u : 2u;
+        S v = A::id();
+        uint32_t it = 0;
+        while (true) {
+          if (exists && flag == 0) flag = peek<S>(a.status, pt, a.epoch, v);
+          if (__all_sync(0xffffffffu, flag != 0)) break;
+          ++it;
+          // Give up (warp-uniformly) after SPIN_LIMIT polls, or at once when
+          // another CTA on this stream has already timed out.
+          bool stop = gave_up || it > SPIN_LIMIT ||
+                      ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
+          if (__any_sync(0xffffffffu, stop)) {
+            gave_up = true;
+            if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
+            if (flag == 0) flag = 2u;  // treat as identity: the result is flagged as failed
+            break;
+          }
+          __nanosleep(it < 8 ? 32 : 128);
+        }
+        const unsigned pmask = __ballot_sync(0xffffffffu, flag == 2u);
+        const int kp = pmask ? __ffs(pmask) - 1 : 32;
+        if (lane > kp) v = A::id();
+        S wv = R2L ? warp_reduce<A>(v) : warp_reduce_rev<A>(v);
+        wv = shfl_idx(wv, 0);
+        acc = R2L ? A::comb(acc, wv) : A::comb(wv, acc);
+        if (pmask) break;
+        k0 += 32;
+      }
+      prefix = acc;
+    }
+    const S inclusive = R2L ? A::comb(bagg, prefix) : A::comb(prefix, bagg);
+    if (lane == 0) {
+      publish<S>(a.status, tile, a.epoch, 2u, inclusive);
+      s_prefix = prefix;
+      const bool last = R2L ? (tile == 0) : (tile == a.ntiles - 1);
+      if (last && a.total_out) *static_cast<T *>(a.total_out) = A::lower(inclusive);
+      if (first && a.seed_out) *static_cast<T *>(a.seed_out) = from_bits<T>(a.seed);
+    }
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- rescan + store
+  S run = R2L ? A::comb(A::comb(excl_lane, wpre), s_prefix) : A::comb(s_prefix, A::comb(wpre, excl_lane));
+  T y[ITEMS];
+  if (!R2L) {
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      if (a.exclusive) { y[j] = A::lower(run); run = A::push(run, x[j]); }
+      else { run = A::push(run, x[j]); y[j] = A::lower(run); }
+    }
+  } else {
+#pragma unroll
+    for (int j = ITEMS - 1; j >= 0; --j) {
+      if (a.exclusive) { y[j] = A::lower(run); run = A::push(run, x[j]); }
+      else { run = A::push(run, x[j]); y[j] = A::lower(run); }
+    }
+  }
+
+  T *dst = static_cast<T *>(a.out);
+  if (a.tma_out) {
+    if (myrow < a.full_rows) {
+#pragma unroll
+      for (int c = 0; c < ITEMS / VEC; ++c) {
+        uint4 v;
+        memcpy(&v, &y[c * VEC], 16);
+        *reinterpret_cast<uint4 *>(buf + swz(tid, c)) = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j)
+        if (e0 + j < a.n) dst[e0 + j] = y[j];
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tma_store_2d(&tout, 0, (int)row0, buf);
+      tma_store_commit();
+      tma_store_wait_read();
+    }
+  } else {
+    __syncthreads();  // every thread has finished reading its row
+#pragma unroll
+    for (int c = 0; c < ITEMS / VEC; ++c) {
+      uint4 v;
+      memcpy(&v, &y[c * VEC], 16);
+      *reinterpret_cast<uint4 *>(buf + swz(tid, c)) = v;
+    }
+    __syncthreads();
+    const int64_t base = tile * (int64_t)TILE;
+    for (int e = tid; e < TILE; e += SCAN_THREADS) {
+      int64_t gi = base + e;
+      if (gi < a.n) {
+        int r = e / ITEMS, k = e % ITEMS;
+        dst[gi] = *reinterpret_cast<const T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T));
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Row scans (rank >= 2): one CTA per row, chunks of 256 x 4 elements with a
+// carried prefix.  in/out rows have pitches in_pitch / out_pitch (elements).
+struct RowScanArgs {
+  const void *in;
+  void *out;
+  void *sums;        // per-row totals (scan') or null
+  int64_t outer, inner;
+  int64_t in_pitch, out_pitch;
+  int64_t out_shift; // 1 for scanl z (output index i+1 holds the inclusive prefix of i), else 0
+  uint64_t seed;
+  int has_seed;
+  int exclusive;
+  int seed_at_end;   // scanr z: out[row][inner] = z
+  int total_at_end;  // scanl z: out[row][inner] = total
+};
+
+template <int OP, class T, int PREC, bool R2L>
+__global__ void __launch_bounds__(256) scan_rows_kernel(RowScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  constexpr int K = 4;
+  constexpr int CH = 256 * K;
+  __shared__ S s_warp[8];
+  __shared__ S s_carry;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T idT = Prim<OP, T>::id();
+  for (int64_t r = blockIdx.x; r < a.outer; r += gridDim.x) {
+    const T *src = static_cast<const T *>(a.in) + r * a.in_pitch;
+    T *dst = static_cast<T *>(a.out) + r * a.out_pitch;
+    if (tid == 0) s_carry = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
+    __syncthreads();
+    const int64_t nch = (a.inner + CH - 1) / CH;
+    for (int64_t ci = 0; ci < nch; ++ci) {
+      const int64_t c = R2L ? nch - 1 - ci : ci;
+      const int64_t e0 = c * CH + (int64_t)tid * K;
+      T x[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) x[j] = e0 + j < a.inner ? src[e0 + j] : idT;
+      S agg;
+      if (!R2L) { agg = A::lift(x[0]); for (int j = 1; j < K; ++j) agg = A::push(agg, x[j]); }
+      else { agg = A::lift(x[K - 1]); for (int j = K - 2; j >= 0; --j) agg = A::push(agg, x[j]); }
+      S incl, ex;
+      if (!R2L) {
+        incl = warp_scan_incl<A>(agg);
+        S up = shfl_up(incl, 1);
+        ex = lane == 0 ? A::id() : up;
+        if (lane == 31) s_warp[warp] = incl;
+      } else {
+        incl = warp_scan_incl_rev<A>(agg);
+        S dn = shfl_down(incl, 1);
+        ex = lane == 31 ? A::id() : dn;
+        if (lane == 0) s_warp[warp] = incl;
+      }
+      __syncthreads();
+      S wpre = A::id();
+      if (!R2L) { for (int w = 0; w < warp; ++w) wpre = A::comb(wpre, s_warp[w]); }
+      else { for (int w = warp + 1; w < 8; ++w) wpre = A::comb(wpre, s_warp[w]); }
+      S bagg = s_warp[0];
+      for (int w = 1; w < 8; ++w) bagg = A::comb(bagg, s_warp[w]);
+      const S carry = s_carry;
+      S run = R2L ? A::comb(A::comb(ex, wpre), carry) : A::comb(carry, A::comb(wpre, ex));
+      if (!R2L) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+          T yv;
+          if (a.exclusive) { yv = A::lower(run); run = A::push(run, x[j]); }
+          else { run = A::push(run, x[j]); yv = A::lower(run); }
+          if (e0 + j < a.inner) dst[e0 + j] = yv;
+        }
+      } else {
+#pragma unroll
+        for (int j = K - 1; j >= 0; --j) {
+          T yv;
+          if (a.exclusive) { yv = A::lower(run); run = A::push(run, x[j]); }
+          else { run = A::push(run, x[j]); yv = A::lower(run); }
+          if (e0 + j < a.inner) dst[e0 + j] = yv;
+        }
+      }
+      __syncthreads();
+      if (tid == 0) s_carry = R2L ? A::comb(bagg, carry) : A::comb(carry, bagg);
+      __syncthreads();
+    }
+    if (tid == 0) {
+      const T total = A::lower(s_carry);
+      if (a.sums) static_cast<T *>(a.sums)[r] = total;
+      if (a.total_at_end) dst[a.inner] = total;
+      if (a.seed_at_end) dst[a.inner] = from_bits<T>(a.seed);
+    }
+    __syncthreads();
+  }
+}
+
+template <class T>
+__global__ void fill_kernel(T *out, int64_t n, uint64_t bits) {
+  const T v = from_bits<T>(bits);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) out[i] = v;
+}
+
+template <class T>
+int launch_fill(T *out, int64_t n, uint64_t bits, cudaStream_t s) {
+  if (n <= 0) return ACC_OK;
+  int64_t blocks = cdiv_h(n, 256);
+  if (blocks > 4096) blocks = 4096;
+  fill_kernel<T><<<(unsigned)blocks, 256, 0, s>>>(out, n, bits);
+  return check_launch();
+}
+template int launch_fill<int32_t>(int32_t *, int64_t, uint64_t, cudaStream_t);
+template int launch_fill<int64_t>(int64_t *, int64_t, uint64_t, cudaStream_t);
+template int launch_fill<uint32_t>(uint32_t *, int64_t, uint64_t, cudaStream_t);
+template int launch_fill<float>(float *, int64_t, uint64_t, cudaStream_t);
+template int launch_fill<double>(double *, int64_t, uint64_t, cudaStream_t);
+
+// ----------------------------------------------------------------- host side
+constexpr size_t SCAN_SMEM = SCAN_THREADS * SCAN_ROW_BYTES + 1024;
+
+template <int OP, class T, int PREC, bool R2L>
+int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
+                   bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  constexpr int64_t TILE = (int64_t)SCAN_THREADS * ITEMS;
+  const int64_t ntiles = cdiv_h(n, TILE);
+  if (ntiles >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
+  int st = ws_status(w, (size_t)ntiles * 2);
+  if (st) return st;
+  ScanArgs a{};
+  a.in = in; a.out = out; a.total_out = total_out; a.seed_out = seed_out;
+  a.n = n;
+  a.full_rows = n / ITEMS;
+  a.ntiles = ntiles;
+  a.seed = seed;
+  a.status = w->status;
+  a.ticket = w->words + W_TICKET;
+  a.err = w->words + W_ERR;
+  a.epoch = ws_next_epoch(w, s);
+  a.has_seed = has_seed;
+  a.exclusive = exclusive;
+  CUtensorMap tin, tout;
+  memset(&tin, 0, sizeof(tin));
+  memset(&tout, 0, sizeof(tout));
+  a.tma_in = a.full_rows > 0 && encode_2d(&tin, in, sizeof(T), ITEMS, a.full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
+  a.tma_out = a.full_rows > 0 && encode_2d(&tout, out, sizeof(T), ITEMS, a.full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
+  auto kern = scan_lookback_kernel<OP, T, PREC, R2L>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SCAN_SMEM);
+    attr_set = true;
+  }
+  kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(tin, tout, a);
+  return check_launch();
+}
+
+template <int OP, class T, int PREC, bool R2L>
+int launch_scan_rows(const RowScanArgs &a, cudaStream_t s) {
+  const Device &d = device_info();
+  int64_t blocks = a.outer;
+  if (blocks > (int64_t)d.sms * 8) blocks = (int64_t)d.sms * 8;
+  scan_rows_kernel<OP, T, PREC, R2L><<<(unsigned)blocks, 256, 0, s>>>(a);
+  return check_launch();
+}
+
+template <int OP, class T, int PREC>
+int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, int64_t outer,
+               int64_t inner, uint64_t seed, cudaStream_t s) {
+  const bool r2l = dir == ACC_R2L;
+  const bool seeded = kind != ACC_SCAN_INCLUSIVE;
+  // Empty innermost extent: scanl/scanr z give [z]; scanl'/scanr' give
+  // ([], z); scanl1/scanr1 give [] (PTX/Execute.hs:386-404,500-512).
+  if (inner == 0) {
+    if (kind == ACC_SCAN_SEEDED) return launch_fill<T>(out, outer, seed, s);
+    if (kind == ACC_SCAN_PRIME) return launch_fill<T>(sums, outer, seed, s);
+    return ACC_OK;
+  }
+  // Output element i lines up with input element i in every flavour:
+  //   scanl z  (L2R, exclusive, total -> out[n])
+  //   scanr z  (R2L, inclusive with the seed on the right, z -> out[n])
+  //   scanl' z (L2R, exclusive, total -> sums), scanr' z (R2L, exclusive, total -> sums)
+  const bool exclusive = kind == ACC_SCAN_PRIME || (kind == ACC_SCAN_SEEDED && !r2l);
+  if (outer == 1) {
+    T *total_out = nullptr, *seed_out = nullptr;
+    if (kind == ACC_SCAN_SEEDED && !r2l) total_out = out + inner;
+    if (kind == ACC_SCAN_SEEDED && r2l) seed_out = out + inner;
+    if (kind == ACC_SCAN_PRIME) total_out = sums;
+    if (r2l) return launch_scan_1d<OP, T, PREC, true>(w, in, out, total_out, seed_out, inner, seeded, exclusive, seed, s);
+    return launch_scan_1d<OP, T, PREC, false>(w, in, out, total_out, seed_out, inner, seeded, exclusive, seed, s);
+  }
+  RowScanArgs a{};
+  a.in = in; a.out = out; a.sums = kind == ACC_SCAN_PRIME ? sums : nullptr;
+  a.outer = outer; a.inner = inner;
+  a.in_pitch = inner;
+  a.out_pitch = kind == ACC_SCAN_SEEDED ? inner + 1 : inner;
+  a.seed = seed; a.has_seed = seeded; a.exclusive = exclusive;
+  a.seed_at_end = kind == ACC_SCAN_SEEDED && r2l;
+  a.total_at_end = kind == ACC_SCAN_SEEDED && !r2l;
+  if (r2l) return launch_scan_rows<OP, T, PREC, true>(a, s);
+  return launch_scan_rows<OP, T, PREC, false>(a, s);
+}
+
+// Exclusive `scanl (+) 0` of segment lengths into offsets (nseg+1 values),
+// used by acc_fold_seg_lengths.
+int scan_offsets(Workspace *w, int type, const void *lengths, void *offsets, int64_t nseg, cudaStream_t s) {
+  if (type == ACC_I32)
+    return launch_scan_1d<ACC_ADD, int32_t, 0, false>(w, (const int32_t *)lengths, (int32_t *)offsets,
+                                                       (int32_t *)offsets + nseg, nullptr, nseg, true, true, 0, s);
+  if (type == ACC_I64)
+    return launch_scan_1d<ACC_ADD, int64_t, 0, false>(w, (const int64_t *)lengths, (int64_t *)offsets,
+                                                       (int64_t *)offsets + nseg, nullptr, nseg, true, true, 0, s);
+  return ACC_ERR_INVALID;
+}
+
+}  // namespace accgb
+
+using namespace accgb;
+
+extern "C" int acc_scan(int op, int type, int prec, int dir, int kind, const void *in, void *out,
+                        void *sums, int64_t outer, int64_t inner, const void *seed, void *stream) {
+  if (outer < 0 || inner < 0) return ACC_ERR_INVALID;
+  if (dir != ACC_L2R && dir != ACC_R2L) return ACC_ERR_INVALID;
+  if (kind < ACC_SCAN_INCLUSIVE || kind > ACC_SCAN_PRIME) return ACC_ERR_INVALID;
+  if (kind != ACC_SCAN_INCLUSIVE && !seed) return ACC_ERR_INVALID;
+  if (outer == 0) return ACC_OK;
+  if (!out && !(inner == 0 && kind != ACC_SCAN_SEEDED)) return ACC_ERR_INVALID;
+  if (inner > 0 && !in) return ACC_ERR_INVALID;
+  if (kind == ACC_SCAN_PRIME && !sums) return ACC_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = ACC_OK;
+  Workspace *w = workspace(s, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  return with_type(type, [&](auto tv) -> int {
+    using T = decltype(tv);
+    const uint64_t sb = seed_bits<T>(seed);
+    return with_op<T>(op, [&](auto opc) -> int {
+      constexpr int OP = decltype(opc)::value;
+      return with_prec<OP, T>(prec, [&](auto pc) -> int {
+        constexpr int P = decltype(pc)::value;
+        return scan_typed<OP, T, P>(w, dir, kind, static_cast<const T *>(in), static_cast<T *>(out),
+                                    static_cast<T *>(sums), outer, inner, sb, s);
+      });
+    });
+  });
+}

@@ -1,0 +1,271 @@
+// stencil.cu -- weighted-sum stencils over rank-1 / rank-2 arrays with
+// clamp / mirror / wrap / constant boundaries.
+//
+// The reference launches `stencil_inside` over the interior (one thread per
+// output, every tap a separate global load, no shared-memory reuse) and
+// 2*rank `stencil_border` kernels on forked streams
+// (accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/PTX/Execute.hs:686-776,
+// PTX/CodeGen/Stencil.hs:113-179).  Here one launch covers the whole array:
+// each CTA pulls a (TH + 2R) x (TW + 2PX) halo tile into shared memory with
+// one 2-D TMA load (the x start rounded out to a 16-byte boundary), CTAs
+// whose halo leaves the array overwrite the out-of-range cells with the
+// boundary rule (accelerate-llvm/src/Data/Array/Accelerate/LLVM/CodeGen/
+// Stencil.hs:195-253), and each thread sweeps a column of TH/4 outputs,
+// keeping one accumulator per output and visiting the taps in the
+// reference's order (rows outer, -r..r; CodeGen/Stencil.hs:73-180).
+//
+// Arithmetic: acc starts at the additive identity and adds w*x per tap,
+// multiply and add rounded separately (no FMA), so Float32 results are
+// bit-identical to a sequential C evaluation of the same expression.  Taps
+// whose weight is exactly zero are not part of the pattern and are not read.
+#include "common.cuh"
+
+namespace accgb {
+
+constexpr int ST_TW = 64;       // tile width (outputs)
+constexpr int ST_TH = 32;       // tile height (outputs)
+constexpr int ST_THREADS = 256; // 64 columns x 4 row groups of 8
+constexpr int ST_ROWS = ST_TH / (ST_THREADS / ST_TW);
+
+template <class T> struct StencilW { T w[81]; };
+
+struct StencilArgs {
+  const void *in;
+  void *out;
+  int64_t h, w;
+  int64_t in_h, in_w;           // extent of the input (boundaries apply here)
+  int64_t in_pitch, out_pitch;  // elements
+  int ry, rx;
+  int boundary;
+  uint64_t cval;
+  int accumulate;  // add onto out (second input of stencil2)
+  int tma;
+  uint32_t *err;
+};
+
+__device__ __forceinline__ int64_t bound_index(int64_t i, int64_t n, int b) {
+  if (i < 0) {
+    if (b == ACC_CLAMP) i = 0;
+    else if (b == ACC_MIRROR) i = -i;
+    else if (b == ACC_WRAP) i = n + i;
+  } else if (i >= n) {
+    if (b == ACC_CLAMP) i = n - 1;
+    else if (b == ACC_MIRROR) i = n - (i - n + 2);
+    else if (b == ACC_WRAP) i = i - n;
+  }
+  // Radii larger than the extent: the reference's remap would step out of
+  // the array again; keep the read inside it.
+  return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+
+template <class T> __device__ __forceinline__ T mul_rn(T a, T b) {
+  if constexpr (std::is_same<T, float>::value) return __fmul_rn(a, b);
+  else if constexpr (std::is_same<T, double>::value) return __dmul_rn(a, b);
+  else { using U = typename IntBits<T>::U; return (T)((U)a * (U)b); }
+}
+
+// RM: the largest radius this instantiation handles (ry, rx <= RM); PX: the
+// halo width in x, RM rounded up to 16 bytes.
+template <class T, int RM>
+__global__ void __launch_bounds__(ST_THREADS)
+stencil_kernel(const __grid_constant__ CUtensorMap tin, StencilArgs a, StencilW<T> W) {
+  constexpr int PX = ((RM * (int)sizeof(T) + 15) / 16) * 16 / (int)sizeof(T);
+  constexpr int SW = ST_TW + 2 * PX;   // smem tile width
+  constexpr int SH = ST_TH + 2 * RM;   // smem tile height
+  extern __shared__ unsigned char smem_raw[];
+  T *tile = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  __shared__ uint64_t bar;
+
+  const int64_t tx0 = (int64_t)blockIdx.x * ST_TW, ty0 = (int64_t)blockIdx.y * ST_TH;
+  const int64_t gx0 = tx0 - PX, gy0 = ty0 - RM;  // global coords of tile[0][0]
+  const T *in = static_cast<const T *>(a.in);
+  const bool border = gx0 < 0 || gy0 < 0 || gx0 + SW > a.in_w || gy0 + SH > a.in_h;
+
+  if (a.tma) {
+    if (threadIdx.x == 0) {
+      mbar_init(&bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      mbar_expect_tx(&bar, SW * SH * sizeof(T));
+      tma_load_2d(tile, &tin, (int)gx0, (int)gy0, &bar);
+    }
+    if (!mbar_wait(&bar, 0)) {
+      raise_error(a.err, DEV_ERR_TIMEOUT);
+      mbar_wait(&bar, 0);
+    }
+    if (border) {
+      // Overwrite the cells the TMA filled with zeros (outside the array).
+      for (int k = threadIdx.x; k < SW * SH; k += ST_THREADS) {
+        const int sy = k / SW, sx = k % SW;
+        const int64_t gy = gy0 + sy, gx = gx0 + sx;
+        if (gy >= 0 && gy < a.in_h && gx >= 0 && gx < a.in_w) continue;
+        T v;
+        if (a.boundary == ACC_CONSTANT) v = from_bits<T>(a.cval);
+        else v = in[bound_index(gy, a.in_h, a.boundary) * a.in_pitch + bound_index(gx, a.in_w, a.boundary)];
+        tile[sy * SW + sx] = v;
+      }
+    }
+  } else {
+    for (int k = threadIdx.x; k < SW * SH; k += ST_THREADS) {
+      const int sy = k / SW, sx = k % SW;
+      const int64_t gy = gy0 + sy, gx = gx0 + sx;
+      T v;
+      if (gy >= 0 && gy < a.in_h && gx >= 0 && gx < a.in_w) v = in[gy * a.in_pitch + gx];
+      else if (a.boundary == ACC_CONSTANT) v = from_bits<T>(a.cval);
+      else v = in[bound_index(gy, a.in_h, a.boundary) * a.in_pitch + bound_index(gx, a.in_w, a.boundary)];
+      tile[sy * SW + sx] = v;
+    }
+  }
+  __syncthreads();
+
+  const int col = threadIdx.x % ST_TW;
+  const int rg = threadIdx.x / ST_TW;
+  const int oy0 = rg * ST_ROWS;  // first output row of this thread (tile coords)
+  T acc[ST_ROWS];
+  T *out = static_cast<T *>(a.out);
+  const int64_t gx = tx0 + col;
+#pragma unroll
+  for (int r = 0; r < ST_ROWS; ++r) {
+    const int64_t gy = ty0 + oy0 + r;
+    if (a.accumulate && gy < a.h && gx < a.w) acc[r] = out[gy * a.out_pitch + gx];
+    else acc[r] = Prim<ACC_ADD, T>::id();
+  }
+  const int ry = a.ry, rx = a.rx;
+  const int KW = 2 * rx + 1;
+  // Input rows oy0-ry .. oy0+ST_ROWS-1+ry (tile coords, offset by RM).
+#pragma unroll
+  for (int ir = 0; ir < ST_ROWS + 2 * RM; ++ir) {
+    const int iy = oy0 + ir - RM;       // input row relative to the tile's first output row
+    const int dyl = ir - RM;            // = iy - oy0
+    if (dyl < -ry || dyl > ST_ROWS - 1 + ry) continue;
+    T xv[2 * RM + 1];
+#pragma unroll
+    for (int dx = -RM; dx <= RM; ++dx)
+      xv[dx + RM] = (dx >= -rx && dx <= rx) ? tile[(iy + RM) * SW + PX + col + dx] : T(0);
+#pragma unroll
+    for (int r = 0; r < ST_ROWS; ++r) {
+      const int dy = dyl - r;  // this input row is tap row dy of output row r
+      if (dy < -ry || dy > ry) continue;
+#pragma unroll
+      for (int dx = -RM; dx <= RM; ++dx) {
+        if (dx < -rx || dx > rx) continue;
+        const T wk = W.w[(dy + ry) * KW + (dx + rx)];
+        if (wk == T(0)) continue;
+        acc[r] = Prim<ACC_ADD, T>::ap(acc[r], mul_rn(wk, xv[dx + RM]));
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < ST_ROWS; ++r) {
+    const int64_t gy = ty0 + oy0 + r;
+    if (gy < a.h && gx < a.w) out[gy * a.out_pitch + gx] = acc[r];
+  }
+}
+
+// ----------------------------------------------------------------- host side
+template <class T, int RM>
+int stencil_launch(StencilArgs a, const StencilW<T> &W, cudaStream_t s) {
+  constexpr int PX = ((RM * (int)sizeof(T) + 15) / 16) * 16 / (int)sizeof(T);
+  constexpr int SW = ST_TW + 2 * PX;
+  constexpr int SH = ST_TH + 2 * RM;
+  const size_t smem = (size_t)SW * SH * sizeof(T) + 128;
+  CUtensorMap tin;
+  memset(&tin, 0, sizeof(tin));
+  a.tma = encode_2d(&tin, a.in, sizeof(T), (uint64_t)a.in_w, (uint64_t)a.in_h, (uint64_t)a.in_pitch * sizeof(T),
+                    SW, SH, false);
+  auto kern = stencil_kernel<T, RM>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int64_t gx = cdiv_h(a.w, ST_TW), gy = cdiv_h(a.h, ST_TH);
+  if (gy > 65535 || gx > (1ll << 31) - 1) return ACC_ERR_TOO_LARGE;
+  kern<<<dim3((unsigned)gx, (unsigned)gy), ST_THREADS, smem, s>>>(tin, a, W);
+  return check_launch();
+}
+
+template <class T>
+int stencil_typed(StencilArgs a, const void *weights, cudaStream_t s) {
+  StencilW<T> W;
+  const int nw = (2 * a.ry + 1) * (2 * a.rx + 1);
+  memset(&W, 0, sizeof(W));
+  memcpy(W.w, weights, (size_t)nw * sizeof(T));
+  const int r = a.ry > a.rx ? a.ry : a.rx;
+  if (r <= 1) return stencil_launch<T, 1>(a, W, s);
+  if (r <= 2) return stencil_launch<T, 2>(a, W, s);
+  return stencil_launch<T, 4>(a, W, s);
+}
+
+static int stencil_dispatch(int type, StencilArgs a, const void *weights, cudaStream_t s) {
+  switch (type) {
+    case ACC_F32: return stencil_typed<float>(a, weights, s);
+    case ACC_F64: return stencil_typed<double>(a, weights, s);
+    case ACC_I32: return stencil_typed<int32_t>(a, weights, s);
+    case ACC_I64: return stencil_typed<int64_t>(a, weights, s);
+    default: return ACC_ERR_UNSUPPORTED;
+  }
+}
+
+static int stencil_check(int type, int ry, int rx, int boundary, const void *cval, int64_t h, int64_t w) {
+  if (ry < 0 || ry > 4 || rx < 0 || rx > 4) return ACC_ERR_INVALID;
+  if (h < 0 || w < 0) return ACC_ERR_INVALID;
+  if (boundary < ACC_CLAMP || boundary > ACC_CONSTANT) return ACC_ERR_INVALID;
+  if (boundary == ACC_CONSTANT && !cval) return ACC_ERR_INVALID;
+  if (type != ACC_F32 && type != ACC_F64 && type != ACC_I32 && type != ACC_I64) return ACC_ERR_UNSUPPORTED;
+  return ACC_OK;
+}
+
+}  // namespace accgb
+
+using namespace accgb;
+
+extern "C" int acc_stencil2d(int type, int ry, int rx, const void *weights, int boundary, const void *cval,
+                             const void *in, void *out, int64_t h, int64_t w, void *stream) {
+  int st = stencil_check(type, ry, rx, boundary, cval, h, w);
+  if (st) return st;
+  if (h == 0 || w == 0) return ACC_OK;
+  if (!weights || !in || !out) return ACC_ERR_INVALID;
+  StencilArgs a{};
+  a.in = in; a.out = out; a.h = h; a.w = w; a.in_h = h; a.in_w = w; a.in_pitch = w; a.out_pitch = w;
+  a.ry = ry; a.rx = rx; a.boundary = boundary;
+  a.cval = 0;
+  if (cval) memcpy(&a.cval, cval, (type == ACC_F64 || type == ACC_I64) ? 8 : 4);
+  a.accumulate = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Workspace *ws = workspace(s, &st);
+  if (!ws) return st;
+  a.err = ws->words + W_ERR;
+  return stencil_dispatch(type, a, weights, s);
+}
+
+extern "C" int acc_stencil2d_pair(int type, int ry, int rx, const void *wa_w, const void *wb_w, int boundary_a,
+                                  const void *cval_a, int boundary_b, const void *cval_b, const void *a_in,
+                                  int64_t ha, int64_t wa, const void *b_in, int64_t hb, int64_t wb, void *out,
+                                  void *stream) {
+  int st = stencil_check(type, ry, rx, boundary_a, cval_a, ha, wa);
+  if (st) return st;
+  st = stencil_check(type, ry, rx, boundary_b, cval_b, hb, wb);
+  if (st) return st;
+  const int64_t h = ha < hb ? ha : hb, w = wa < wb ? wa : wb;
+  if (h == 0 || w == 0) return ACC_OK;
+  if (!wa_w || !wb_w || !a_in || !b_in || !out) return ACC_ERR_INVALID;
+  const size_t esz = (type == ACC_F64 || type == ACC_I64) ? 8 : 4;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Workspace *ws = workspace(s, &st);
+  if (!ws) return st;
+  // Pass 1 evaluates the taps of a; pass 2 continues the same accumulator
+  // (read back from out) with the taps of b.  The accumulator is rounded to
+  // the element type after every tap either way, so the two passes give the
+  // bits of one fused sweep.
+  StencilArgs a{};
+  a.err = ws->words + W_ERR;
+  a.in = a_in; a.out = out; a.h = h; a.w = w; a.in_h = ha; a.in_w = wa; a.in_pitch = wa; a.out_pitch = w;
+  a.ry = ry; a.rx = rx; a.boundary = boundary_a; a.cval = 0;
+  if (cval_a) memcpy(&a.cval, cval_a, esz);
+  a.accumulate = 0;
+  st = stencil_dispatch(type, a, wa_w, s);
+  if (st) return st;
+  a.in = b_in; a.in_h = hb; a.in_w = wb; a.in_pitch = wb; a.boundary = boundary_b; a.cval = 0;
+  if (cval_b) memcpy(&a.cval, cval_b, esz);
+  a.accumulate = 1;
+  return stencil_dispatch(type, a, wb_w, s);
+}

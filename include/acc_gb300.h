@@ -1,0 +1,243 @@
+/*
+ * acc_gb300.h -- C ABI of the GB300 (sm_103a) skeleton library `libaccgb.so`.
+ *
+ * These entry points replace the bodies of the `Execute PTX` skeleton
+ * operations of accelerate-llvm-ptx (instance at
+ * accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/PTX/Execute.hs:83-109)
+ * for the fixed associative primitives (+ * min max .&. .|. xor) over
+ * Int32 / Int64 / Word32 / Float32 / Float64.  Every kernel behind them is
+ * hand-written CUDA for sm_103a; there is no CPU fallback.
+ *
+ * Conventions (carried over from the reference runtime):
+ *  - Ownership: the caller owns every input and output buffer (device
+ *    pointers).  The library owns and caches its temporaries per stream, as the
+ *    reference allocates its temps with `allocateRemote`
+ *    (PTX/Execute.hs:313,453).
+ *  - Asynchrony: work is enqueued on `stream` (a cudaStream_t, passed as
+ *    void*; NULL = the legacy default stream) and the call returns at once,
+ *    like the reference's `Par PTX (Future ...)` ops which record an event
+ *    after the launch (PTX/Execute/Async.hs:115-126,175-187).  Device-side
+ *    failures (a bounded wait that ran out, an out-of-range permutation index)
+ *    are raised into a per-stream error word and reported by acc_sync().
+ *  - Errors: every call returns an acc_status; nothing aborts.  A Haskell shim
+ *    maps non-zero codes to `internalError`, as `evalPTX` does
+ *    (PTX/State.hs:51-55).
+ *  - Layout: row-major, innermost dimension contiguous (SoA components of a
+ *    tuple are separate calls).  `outer` is the product of all but the
+ *    innermost extent and `inner` the innermost extent; extents are int64 as
+ *    the reference marshals `Int` (PTX/Execute/Marshal.hs:49).
+ *  - Seeds: `seed` points to ONE host-memory element of the array's type, or
+ *    is NULL for the seedless variant (fold1, scanl1, ...).  The seed is
+ *    combined on the LEFT for left-to-right operations (z `f` x0 ...) and on
+ *    the RIGHT for right-to-left scans (... x(n-1) `f` z), as in
+ *    accelerate-llvm-native/.../Native/CodeGen/Fold.hs:256-260 and
+ *    Native/CodeGen/Scan.hs:190-205.
+ */
+#ifndef ACC_GB300_H
+#define ACC_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACC_GB300_ABI_VERSION 1
+
+/* Element types: the scalar types of Accelerate's `ScalarType` that the
+ * skeleton layer supports (Int32, Int64, Word32, Float, Double). */
+typedef enum acc_type {
+  ACC_I32 = 0,
+  ACC_I64 = 1,
+  ACC_U32 = 2,
+  ACC_F32 = 3,
+  ACC_F64 = 4
+} acc_type;
+
+/* The fixed associative primitives recognised by the shim, the same set the
+ * reference turns into atomic RMW operations (accelerate-llvm/src/Data/Array/
+ * Accelerate/LLVM/CodeGen/Permute.hs:136-160).  Integer + and * wrap
+ * (LLVM/AST/Type/Instruction.hs:429-473); float min/max are IEEE fmin/fmax,
+ * integer min/max are `select` on <= / >= (CodeGen/Arithmetic.hs:456-466);
+ * the bitwise primitives exist for the integral types only. */
+typedef enum acc_op {
+  ACC_ADD = 0,
+  ACC_MUL = 1,
+  ACC_MIN = 2,
+  ACC_MAX = 3,
+  ACC_AND = 4,
+  ACC_OR  = 5,
+  ACC_XOR = 6
+} acc_op;
+
+/* Float32 accumulation policy of fold / foldSeg / scan with (+).
+ * COMPENSATED (the default for Float32 +) carries a two-sum error term in
+ * FP32; PLAIN is an FP32 tree; FP64ACC accumulates in FP64 and rounds once.
+ * Ignored for every other (op, type) pair. */
+typedef enum acc_prec {
+  ACC_PREC_DEFAULT     = 0,
+  ACC_PREC_PLAIN       = 1,
+  ACC_PREC_COMPENSATED = 2,
+  ACC_PREC_FP64ACC     = 3
+} acc_prec;
+
+/* Scan direction (Accelerate `Direction`: LeftToRight / RightToLeft). */
+typedef enum acc_dir { ACC_L2R = 0, ACC_R2L = 1 } acc_dir;
+
+/* Scan flavour (accelerate-llvm/src/.../LLVM/Execute.hs:93-156,
+ * `scan` True/False and `scan'`). */
+typedef enum acc_scan_kind {
+  ACC_SCAN_INCLUSIVE = 0, /* scanl1 / scanr1: out has n elements, seed unused           */
+  ACC_SCAN_SEEDED    = 1, /* scanl z / scanr z: out has n+1 elements                    */
+  ACC_SCAN_PRIME     = 2  /* scanl' z / scanr' z: out has n elements, total -> `sums`   */
+} acc_scan_kind;
+
+/* Stencil boundary conditions (accelerate-llvm/.../CodeGen/Stencil.hs:207-253).
+ * The user-function boundary is out of scope. */
+typedef enum acc_boundary {
+  ACC_CLAMP    = 0,
+  ACC_MIRROR   = 1,
+  ACC_WRAP     = 2,
+  ACC_CONSTANT = 3
+} acc_boundary;
+
+typedef enum acc_status {
+  ACC_OK              = 0,
+  ACC_ERR_INVALID     = 1, /* bad argument (null pointer, negative extent, bad enum) */
+  ACC_ERR_UNSUPPORTED = 2, /* (op, type) pair outside the fixed primitives          */
+  ACC_ERR_EMPTY       = 3, /* fold1 / foldSeg-without-seed over an empty extent      */
+  ACC_ERR_CUDA        = 4, /* a CUDA runtime call failed                             */
+  ACC_ERR_NOMEM       = 5, /* device allocation of a temporary failed                */
+  ACC_ERR_TIMEOUT     = 6, /* a bounded device wait ran out (reported by acc_sync)   */
+  ACC_ERR_INDEX       = 7, /* permute index >= size of the target (acc_sync)         */
+  ACC_ERR_TOO_LARGE   = 8  /* an extent beyond what the entry point accepts          */
+} acc_status;
+
+/* ---------------------------------------------------------------- library */
+
+/* ABI version (ACC_GB300_ABI_VERSION). */
+int acc_version(void);
+
+/* Human-readable text of a status code (static storage). */
+const char *acc_strerror(int status);
+
+/* Wait for all work enqueued on `stream`, then return and clear the device
+ * error word of that stream (ACC_OK, ACC_ERR_TIMEOUT, ACC_ERR_INDEX) or
+ * ACC_ERR_CUDA if the stream itself failed.  Plays the part of the
+ * reference's `get`/`block` on a Future (PTX/Execute/Async.hs:132-165). */
+int acc_sync(void *stream);
+
+/* Drop the cached temporaries of every stream (they are re-made on demand). */
+int acc_release_workspaces(void);
+
+/* ---------------------------------------------------------------- fold */
+
+/* fold f z / fold1 f along the innermost dimension.
+ * Replaces foldOp / fold1Op / foldCore / foldAllOp / foldDimOp
+ * (PTX/Execute.hs:222-340).
+ *   in  : outer*inner elements, out : outer elements.
+ *   seed: NULL => fold1 (inner must be >= 1 unless outer*inner == 0,
+ *         otherwise ACC_ERR_EMPTY as `boundsCheck "empty array"`,
+ *         PTX/Execute.hs:232).  inner == 0 with a seed fills out with z
+ *         (PTX/Execute.hs:248). */
+int acc_fold(int op, int type, int prec, const void *in, void *out,
+             int64_t outer, int64_t inner, const void *seed, void *stream);
+
+/* ---------------------------------------------------------------- foldSeg */
+
+/* foldSeg f z / fold1Seg f over a segment-OFFSET array (length nseg+1, the
+ * `scanl (+) 0` of the lengths, as the reference receives it,
+ * PTX/Execute.hs:343-374 "segments array has been 'scanl (+) 0'`ed").
+ * Replaces foldSegOp.
+ *   in: outer*inner elements; offsets: nseg+1 values of `offset_type`
+ *   (ACC_I32 or ACC_I64), non-decreasing, 0 <= offsets[i] <= inner;
+ *   out: outer*nseg elements.
+ *   An empty segment gives z with a seed and is left unwritten without one
+ *   (PTX/CodeGen/FoldSeg.hs:170-178). */
+int acc_fold_seg(int op, int type, int prec, const void *in,
+                 const void *offsets, int offset_type, void *out,
+                 int64_t outer, int64_t inner, int64_t nseg,
+                 const void *seed, void *stream);
+
+/* foldSeg over segment LENGTHS: first computes the offsets with the
+ * library's own single-pass scan (what the Accelerate frontend does before
+ * the backend sees the array), then runs acc_fold_seg. */
+int acc_fold_seg_lengths(int op, int type, int prec, const void *in,
+                         const void *lengths, int length_type, void *out,
+                         int64_t outer, int64_t inner, int64_t nseg,
+                         const void *seed, void *stream);
+
+/* ---------------------------------------------------------------- scan */
+
+/* scanl / scanl1 / scanr / scanr1 / scanl' / scanr' along the innermost
+ * dimension.  Replaces scanOp / scan1Op / scan'Op / scanCore / scanAllOp /
+ * scanDimOp (PTX/Execute.hs:377-594).
+ *   in : outer*inner elements.
+ *   out: outer*inner elements (INCLUSIVE, PRIME) or outer*(inner+1)
+ *        (SEEDED: scanl z puts z at index 0, scanr z puts it at index n).
+ *   sums: outer elements for PRIME (the per-row totals), else ignored.
+ *   seed: required for SEEDED and PRIME, ignored for INCLUSIVE. */
+int acc_scan(int op, int type, int prec, int dir, int kind, const void *in,
+             void *out, void *sums, int64_t outer, int64_t inner,
+             const void *seed, void *stream);
+
+/* ---------------------------------------------------------------- permute */
+
+/* permute f defaults p xs, for the fixed primitives.  Replaces permuteOp +
+ * permute_rmw (PTX/Execute.hs:597-649; PTX/CodeGen/Permute.hs:117-213).
+ *   out : m elements, ALREADY holding the defaults (the reference clones the
+ *         defaults first, PTX/Execute.hs:623-625; acc_permute_clone does it).
+ *   src : n source values, or NULL to combine the constant *cval (host
+ *         pointer to one element) for every source index (the fused
+ *         `fill n c` producer of a histogram).
+ *   idx : n target indices of `index_type` (ACC_I32 / ACC_I64); a negative
+ *         index is `Nothing` (the element is dropped); an index >= m is
+ *         dropped and raises ACC_ERR_INDEX at the next acc_sync.
+ *   Each update is out[j] = f x out[j] (new value first,
+ *   Native/CodeGen/Permute.hs:112-116).  Integer results are exact under any
+ *   order; Float32/Float64 (+ and *) depend on the update order. */
+int acc_permute(int op, int type, const void *src, const void *cval,
+                const void *idx, int index_type, void *out, int64_t n,
+                int64_t m, void *stream);
+
+/* Clone `defaults` (m elements) into `out`, then acc_permute. */
+int acc_permute_clone(int op, int type, const void *defaults, const void *src,
+                      const void *cval, const void *idx, int index_type,
+                      void *out, int64_t n, int64_t m, void *stream);
+
+/* ---------------------------------------------------------------- stencil */
+
+/* stencil over a rank-2 (or rank-1 with h == 1, ry == 0) array with a
+ * weighted-sum stencil function:
+ *     out[y][x] = sum_{dy=-ry..ry, dx=-rx..rx} w[(dy+ry)*(2rx+1)+(dx+rx)] * in[y+dy][x+dx]
+ * accumulated in that tap order (rows outer, -r..r, as the reference's
+ * stencil access, accelerate-llvm/.../CodeGen/Stencil.hs:73-180), without
+ * fused multiply-add, starting from w[0]*x[0].  Out-of-range reads follow
+ * `boundary` (CodeGen/Stencil.hs:207-253); `cval` (host pointer) is the
+ * constant of ACC_CONSTANT.  Types ACC_F32 / ACC_F64 (float weights) and
+ * ACC_I32 / ACC_I64 (integer weights, wrapping).  rx, ry in [0, 4]
+ * (the reference's largest stencil pattern is 9 wide).  `weights` is a HOST
+ * pointer to (2ry+1)(2rx+1) elements of `type`.
+ * Replaces stencil1Op / stencilCore (PTX/Execute.hs:652-748). */
+int acc_stencil2d(int type, int ry, int rx, const void *weights, int boundary,
+                  const void *cval, const void *in, void *out, int64_t h,
+                  int64_t w, void *stream);
+
+/* stencil2: two inputs a (ha x wa) and b (hb x wb), out = stencil(a, wa_w)
+ * followed by the taps of stencil(b, wb_w) in the same accumulator, over the
+ * intersection min(ha,hb) x min(wa,wb) of the shapes (PTX/Execute.hs:682,
+ * `intersect`).  Each input's boundary applies at that input's own extent, as
+ * each delayed input is bounded by its own shape (CodeGen/Stencil.hs:201-210).
+ * Replaces stencil2Op (PTX/Execute.hs:669-684). */
+int acc_stencil2d_pair(int type, int ry, int rx, const void *wa_w,
+                       const void *wb_w, int boundary_a, const void *cval_a,
+                       int boundary_b, const void *cval_b, const void *a,
+                       int64_t ha, int64_t wa, const void *b, int64_t hb,
+                       int64_t wb, void *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACC_GB300_H */

@@ -1,0 +1,531 @@
+/*
+ * oracle.c -- CPU restatement of accelerate-llvm-native's skeleton semantics.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library
+ * (tests/, __graft_entry__.smoke()) and the timed CPU baseline of bench.py
+ * (its `cpu_baseline` leg and `--impl reference`).  Nothing in the product
+ * path links, loads or calls it.
+ *
+ * The reference CPU backend (accelerate-llvm-native) is Haskell that emits
+ * LLVM IR at run time; it cannot be built here (no GHC, no clang, and the
+ * `accelerate` core package it depends on is not vendored).  This file
+ * restates, function by function, what its generated code computes:
+ *
+ *  - primitives: integer + * wrap (accelerate-llvm/src/LLVM/AST/Type/
+ *    Instruction.hs:429-473, no nsw/nuw); integer min/max select on <= / >=,
+ *    float min/max are fmin/fmax (accelerate-llvm/src/Data/Array/Accelerate/
+ *    LLVM/CodeGen/Arithmetic.hs:456-466); no fast-math, no FMA contraction
+ *    (this file must be compiled with -ffp-contract=off).
+ *  - fold / fold1: left fold from the seed, z `f` x0 `f` x1 ...
+ *    (accelerate-llvm-native/src/Data/Array/Accelerate/LLVM/Native/CodeGen/
+ *    Fold.hs:74-100, reduceFromTo / reduce1FromTo :248-275).  A parallel
+ *    whole-array fold reduces the pieces of divideWork1 (splits = workers-1,
+ *    minsize 4096) and then the piece results left to right from the seed
+ *    (Native/Execute.hs:294-333, Native/Execute/Divide.hs:67-104).
+ *  - foldSeg: per segment i, fold over [seg[i], seg[i+1]) of the row
+ *    (Native/CodeGen/FoldSeg.hs:103-141).
+ *  - scan family: Native/CodeGen/Scan.hs:136-270 (scanS, scan'S): L2R combines
+ *    `f acc x`, R2L `f x acc`; scanl z writes z first, scanr z writes z at
+ *    index n; scan' writes the carry-in before combining.  Parallel 1-D scans
+ *    (n >= 8192) use divideWork pieces of minsize 8192 and a three-phase
+ *    scan (Native/Execute.hs:456-467, Scan.hs:294-491).
+ *  - permute: out[p i] = f (x i) (out[p i]) with the new value first
+ *    (Native/CodeGen/Permute.hs:85-118); a negative index is `Nothing`.
+ *  - stencil: taps rows outer, -r..r (accelerate-llvm/.../CodeGen/
+ *    Stencil.hs:73-180); boundaries clamp / mirror / wrap / constant
+ *    (CodeGen/Stencil.hs:195-253).  The stencil function is a weighted sum
+ *    accumulated from the additive identity in tap order, multiply and add
+ *    rounded separately; zero-weight taps are not part of the pattern.
+ *
+ * Besides the restatement in the element type, *_f64 variants compute float
+ * folds / scans / segmented folds in FP64 with Neumaier compensation: the
+ * FP64 oracle against which Float32 errors are stated.
+ *
+ * Parity pins: the reference ships two known answers for this path,
+ * `sum (map (+1) [1..10000]) == 50015000` (accelerate-llvm-ptx/test/nofib/
+ * Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs:26-31) and
+ * `scanl (+) 10 [0..9] == [10,10,11,13,16,20,25,31,38,46,55]`
+ * (accelerate-llvm-native/.../Native/CodeGen/Scan.hs:50-56); tests/ checks
+ * this oracle against both.  The core package's property suite is not in the
+ * tree, so the other (op, type, skeleton) cases are pinned only by this
+ * restatement: parity partially pinned.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+enum { T_I32 = 0, T_I64 = 1, T_U32 = 2, T_F32 = 3, T_F64 = 4 };
+enum { O_ADD = 0, O_MUL, O_MIN, O_MAX, O_AND, O_OR, O_XOR };
+enum { OK = 0, E_INVALID = 1, E_UNSUPPORTED = 2, E_EMPTY = 3, E_NOMEM = 5, E_INDEX = 7 };
+
+static int orc_tnum(void) {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+int orc_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ work split
+ * divideWork1 (Native/Execute/Divide.hs:67-104): recursively halve [from, to)
+ * `splits` levels deep; the split point is rounded up to a multiple of
+ * minsize.  Pieces of at least minsize come first, the smaller ones after;
+ * `index` numbers the pieces left to right. */
+typedef struct { int64_t u, v, index; } piece;
+
+static void split1(int64_t s, int64_t u, int64_t v, int64_t minsize, int64_t *i, piece *full, int64_t *nf,
+                   piece *small, int64_t *ns) {
+  if (s == 0) {
+    piece p = {u, v, (*i)++};
+    if (v - u < minsize) small[(*ns)++] = p; else full[(*nf)++] = p;
+    return;
+  }
+  int64_t a = v - u;
+  if (a <= minsize) {
+    piece p = {u, v, (*i)++};
+    small[(*ns)++] = p;
+    return;
+  }
+  int64_t b = (a + 1) >> 1, c = minsize - 1, d = (b + c) & ~c;
+  split1(s >> 1, u, d + u, minsize, i, full, nf, small, ns);
+  split1(s >> 1, d + u, v, minsize, i, full, nf, small, ns);
+}
+
+/* Returns the number of pieces written to out (3 int64 each: u, v, index). */
+int64_t orc_divide_work1(int64_t splits, int64_t minsize, int64_t from, int64_t to, int64_t *out, int64_t max) {
+  int64_t cap = 2 * (splits + 2) + 8;
+  piece *full = malloc(sizeof(piece) * cap), *small = malloc(sizeof(piece) * cap);
+  int64_t nf = 0, ns = 0, i = 0;
+  split1(splits, from, to, minsize, &i, full, &nf, small, &ns);
+  int64_t k = 0;
+  for (int64_t j = 0; j < nf && k < max; ++j, ++k) { out[3 * k] = full[j].u; out[3 * k + 1] = full[j].v; out[3 * k + 2] = full[j].index; }
+  for (int64_t j = 0; j < ns && k < max; ++j, ++k) { out[3 * k] = small[j].u; out[3 * k + 1] = small[j].v; out[3 * k + 2] = small[j].index; }
+  free(full); free(small);
+  return k;
+}
+
+/* Pieces sorted by their left-to-right index. */
+static int64_t pieces_in_order(int64_t splits, int64_t minsize, int64_t n, piece **out) {
+  int64_t cap = 2 * (splits + 2) + 8;
+  int64_t *raw = malloc(sizeof(int64_t) * 3 * cap);
+  int64_t k = orc_divide_work1(splits, minsize, 0, n, raw, cap);
+  piece *p = malloc(sizeof(piece) * (k ? k : 1));
+  for (int64_t j = 0; j < k; ++j) {
+    int64_t idx = raw[3 * j + 2];
+    p[idx].u = raw[3 * j]; p[idx].v = raw[3 * j + 1]; p[idx].index = idx;
+  }
+  free(raw);
+  *out = p;
+  return k;
+}
+
+/* ------------------------------------------------------------------ primitives */
+#define I_ADD(T, U, a, b) ((T)((U)(a) + (U)(b)))
+#define I_MUL(T, U, a, b) ((T)((U)(a) * (U)(b)))
+#define I_MIN(T, U, a, b) ((a) <= (b) ? (a) : (b))
+#define I_MAX(T, U, a, b) ((a) >= (b) ? (a) : (b))
+#define I_AND(T, U, a, b) ((a) & (b))
+#define I_OR(T, U, a, b) ((a) | (b))
+#define I_XOR(T, U, a, b) ((a) ^ (b))
+#define F_ADD(T, U, a, b) ((T)((a) + (b)))
+#define F_MUL(T, U, a, b) ((T)((a) * (b)))
+#define F_MINf(T, U, a, b) fminf((a), (b))
+#define F_MAXf(T, U, a, b) fmaxf((a), (b))
+#define F_MINd(T, U, a, b) fmin((a), (b))
+#define F_MAXd(T, U, a, b) fmax((a), (b))
+
+/* One set of skeleton bodies per (type, primitive). */
+#define DEFINE_SKELETONS(NAME, T, U, COMB)                                                                   \
+  static T NAME##_c(T a, T b) { return COMB(T, U, a, b); }                                                   \
+  static void NAME##_fold(const T *in, T *out, int64_t outer, int64_t inner, const T *seed, int nth) {     \
+    if (outer == 1 && nth > 1 && inner >= 2 * 4096) {                                                        \
+      piece *ps; int64_t np = pieces_in_order(nth - 1, 4096, inner, &ps);                                   \
+      T *tmp = malloc(sizeof(T) * np);                                                                       \
+      _Pragma("omp parallel for schedule(dynamic, 1)")                                                       \
+      for (int64_t k = 0; k < np; ++k) {                                                                     \
+        T acc = in[ps[k].u];                                                                                 \
+        for (int64_t i = ps[k].u + 1; i < ps[k].v; ++i) acc = NAME##_c(acc, in[i]);                          \
+        tmp[k] = acc;                                                                                        \
+      }                                                                                                      \
+      T acc = seed ? *seed : tmp[0];                                                                         \
+      for (int64_t k = seed ? 0 : 1; k < np; ++k) acc = NAME##_c(acc, tmp[k]);                               \
+      out[0] = acc;                                                                                          \
+      free(tmp); free(ps);                                                                                   \
+      return;                                                                                                \
+    }                                                                                                        \
+    _Pragma("omp parallel for schedule(static) if (nth > 1 && outer > 1)")                                   \
+    for (int64_t r = 0; r < outer; ++r) {                                                                    \
+      const T *p = in + r * inner;                                                                           \
+      T acc = seed ? *seed : p[0];                                                                           \
+      for (int64_t i = seed ? 0 : 1; i < inner; ++i) acc = NAME##_c(acc, p[i]);                              \
+      out[r] = acc;                                                                                          \
+    }                                                                                                        \
+  }                                                                                                          \
+  static void NAME##_foldseg(const T *in, const void *off, int off64, T *out, int64_t outer, int64_t inner, \
+                             int64_t nseg, const T *seed, int nth, int *bad) {                               \
+    int b = 0;                                                                                               \
+    _Pragma("omp parallel for schedule(static) reduction(|: b) if (nth > 1)")                                \
+    for (int64_t j = 0; j < outer * nseg; ++j) {                                                             \
+      int64_t r = j / nseg, s = j % nseg;                                                                    \
+      int64_t u = off64 ? ((const int64_t *)off)[s] : ((const int32_t *)off)[s];                             \
+      int64_t v = off64 ? ((const int64_t *)off)[s + 1] : ((const int32_t *)off)[s + 1];                     \
+      if (u < 0 || v < u || v > inner) { b = 1; continue; }                                                  \
+      const T *p = in + r * inner;                                                                           \
+      if (v == u && !seed) continue;                                                                         \
+      T acc = seed ? *seed : p[u];                                                                           \
+      for (int64_t i = seed ? u : u + 1; i < v; ++i) acc = NAME##_c(acc, p[i]);                              \
+      out[r * nseg + s] = acc;                                                                               \
+    }                                                                                                        \
+    *bad = b;                                                                                                \
+  }                                                                                                          \
+  /* Sequential scan of one row, Native/CodeGen/Scan.hs:136-270. */                                         \
+  static void NAME##_scan_row(const T *in, T *out, T *sum, int64_t n, int r2l, int kind, const T *seed) {   \
+    if (kind == 1) { /* scanl z / scanr z: n+1 outputs */                                                    \
+      if (!r2l) {                                                                                            \
+        T acc = *seed; out[0] = acc;                                                                         \
+        for (int64_t i = 0; i < n; ++i) { acc = NAME##_c(acc, in[i]); out[i + 1] = acc; }                    \
+      } else {                                                                                               \
+        T acc = *seed; out[n] = acc;                                                                         \
+        for (int64_t i = n - 1; i >= 0; --i) { acc = NAME##_c(in[i], acc); out[i] = acc; }                   \
+      }                                                                                                      \
+    } else if (kind == 2) { /* scan' z: carry-in written before combining */                                 \
+      T acc = *seed;                                                                                         \
+      if (!r2l) for (int64_t i = 0; i < n; ++i) { out[i] = acc; acc = NAME##_c(acc, in[i]); }                \
+      else for (int64_t i = n - 1; i >= 0; --i) { out[i] = acc; acc = NAME##_c(in[i], acc); }                \
+      *sum = acc;                                                                                            \
+    } else if (n > 0) { /* scanl1 / scanr1 */                                                                \
+      if (!r2l) { T acc = in[0]; out[0] = acc; for (int64_t i = 1; i < n; ++i) { acc = NAME##_c(acc, in[i]); out[i] = acc; } } \
+      else { T acc = in[n - 1]; out[n - 1] = acc; for (int64_t i = n - 2; i >= 0; --i) { acc = NAME##_c(in[i], acc); out[i] = acc; } } \
+    }                                                                                                        \
+  }                                                                                                          \
+  /* Three-phase parallel scanl1 / scanl of a vector over divideWork pieces. */                             \
+  static void NAME##_scan_par(const T *in, T *out, int64_t n, int kind, const T *seed, int nth) {           \
+    piece *ps; int64_t np = pieces_in_order(nth - 1, 8192, n, &ps);                                         \
+    T *tot = malloc(sizeof(T) * np);                                                                         \
+    const int64_t sh = kind == 1 ? 1 : 0;                                                                    \
+    _Pragma("omp parallel for schedule(dynamic, 1)")                                                         \
+    for (int64_t k = 0; k < np; ++k) {                                                                       \
+      T acc = in[ps[k].u]; out[ps[k].u + sh] = acc;                                                          \
+      for (int64_t i = ps[k].u + 1; i < ps[k].v; ++i) { acc = NAME##_c(acc, in[i]); out[i + sh] = acc; }     \
+      tot[k] = acc;                                                                                          \
+    }                                                                                                        \
+    T carry = seed ? *seed : tot[0];                                                                         \
+    if (kind == 1) out[0] = *seed;                                                                           \
+    T *cin = malloc(sizeof(T) * np);                                                                         \
+    for (int64_t k = 0; k < np; ++k) {                                                                       \
+      if (k == 0) { cin[k] = seed ? *seed : tot[0]; if (seed) carry = NAME##_c(*seed, tot[0]); }            \
+      else { cin[k] = carry; carry = NAME##_c(carry, tot[k]); }                                              \
+    }                                                                                                        \
+    _Pragma("omp parallel for schedule(dynamic, 1)")                                                         \
+    for (int64_t k = 0; k < np; ++k) {                                                                       \
+      if (k == 0 && !seed) continue;                                                                         \
+      for (int64_t i = ps[k].u; i < ps[k].v; ++i) out[i + sh] = NAME##_c(cin[k], out[i + sh]);               \
+    }                                                                                                        \
+    free(cin); free(tot); free(ps);                                                                          \
+  }                                                                                                          \
+  static void NAME##_scan(const T *in, T *out, T *sums, int64_t outer, int64_t inner, int r2l, int kind,    \
+                          const T *seed, int nth) {                                                          \
+    const int64_t op = kind == 1 ? inner + 1 : inner;                                                       \
+    if (outer == 1 && nth > 1 && !r2l && kind != 2 && inner >= 8192) {                                       \
+      NAME##_scan_par(in, out, inner, kind, seed, nth);                                                      \
+      return;                                                                                                \
+    }                                                                                                        \
+    _Pragma("omp parallel for schedule(static) if (nth > 1 && outer > 1)")                                   \
+    for (int64_t r = 0; r < outer; ++r)                                                                      \
+      NAME##_scan_row(in + r * inner, out + r * op, sums ? sums + r : 0, inner, r2l, kind, seed);            \
+  }                                                                                                          \
+  static void NAME##_permute(const T *src, const T *cval, const void *idx, int idx64, T *out, int64_t n,    \
+                             int64_t m, int nth, int *bad) {                                                 \
+    int b = 0;                                                                                               \
+    if (nth <= 1 || (double)m * nth * sizeof(T) > 512e6) {                                                   \
+      for (int64_t i = 0; i < n; ++i) {                                                                      \
+        int64_t j = idx64 ? ((const int64_t *)idx)[i] : ((const int32_t *)idx)[i];                           \
+        if (j < 0) continue;                                                                                 \
+        if (j >= m) { b = 1; continue; }                                                                     \
+        out[j] = NAME##_c(src ? src[i] : *cval, out[j]);                                                     \
+      }                                                                                                      \
+      *bad = b;                                                                                              \
+      return;                                                                                                \
+    }                                                                                                        \
+    /* Parallel: private targets per thread, folded in thread order. */                                     \
+    T **priv = calloc(nth, sizeof(T *));                                                                     \
+    char **touched = calloc(nth, sizeof(char *));                                                            \
+    _Pragma("omp parallel num_threads(nth) reduction(|: b)")                                                 \
+    {                                                                                                        \
+      const int t = orc_tnum();                                                                              \
+      T *pv = malloc(sizeof(T) * (m ? m : 1));                                                               \
+      char *tc = calloc(m ? m : 1, 1);                                                                       \
+      priv[t] = pv; touched[t] = tc;                                                                         \
+      _Pragma("omp for schedule(static)")                                                                    \
+      for (int64_t i = 0; i < n; ++i) {                                                                      \
+        int64_t j = idx64 ? ((const int64_t *)idx)[i] : ((const int32_t *)idx)[i];                           \
+        if (j < 0) continue;                                                                                 \
+        if (j >= m) { b = 1; continue; }                                                                     \
+        T x = src ? src[i] : *cval;                                                                          \
+        if (tc[j]) pv[j] = NAME##_c(x, pv[j]); else { pv[j] = x; tc[j] = 1; }                                \
+      }                                                                                                      \
+    }                                                                                                        \
+    _Pragma("omp parallel for schedule(static)")                                                             \
+    for (int64_t j = 0; j < m; ++j)                                                                          \
+      for (int t = 0; t < nth; ++t)                                                                     \
+        if (touched[t] && touched[t][j]) out[j] = NAME##_c(priv[t][j], out[j]);                              \
+    for (int t = 0; t < nth; ++t) { free(priv[t]); free(touched[t]); }                                       \
+    free(priv); free(touched);                                                                               \
+    *bad = b;                                                                                                \
+  }
+
+DEFINE_SKELETONS(i32_add, int32_t, uint32_t, I_ADD)
+DEFINE_SKELETONS(i32_mul, int32_t, uint32_t, I_MUL)
+DEFINE_SKELETONS(i32_min, int32_t, uint32_t, I_MIN)
+DEFINE_SKELETONS(i32_max, int32_t, uint32_t, I_MAX)
+DEFINE_SKELETONS(i32_and, int32_t, uint32_t, I_AND)
+DEFINE_SKELETONS(i32_or, int32_t, uint32_t, I_OR)
+DEFINE_SKELETONS(i32_xor, int32_t, uint32_t, I_XOR)
+DEFINE_SKELETONS(i64_add, int64_t, uint64_t, I_ADD)
+DEFINE_SKELETONS(i64_mul, int64_t, uint64_t, I_MUL)
+DEFINE_SKELETONS(i64_min, int64_t, uint64_t, I_MIN)
+DEFINE_SKELETONS(i64_max, int64_t, uint64_t, I_MAX)
+DEFINE_SKELETONS(i64_and, int64_t, uint64_t, I_AND)
+DEFINE_SKELETONS(i64_or, int64_t, uint64_t, I_OR)
+DEFINE_SKELETONS(i64_xor, int64_t, uint64_t, I_XOR)
+DEFINE_SKELETONS(u32_add, uint32_t, uint32_t, I_ADD)
+DEFINE_SKELETONS(u32_mul, uint32_t, uint32_t, I_MUL)
+DEFINE_SKELETONS(u32_min, uint32_t, uint32_t, I_MIN)
+DEFINE_SKELETONS(u32_max, uint32_t, uint32_t, I_MAX)
+DEFINE_SKELETONS(u32_and, uint32_t, uint32_t, I_AND)
+DEFINE_SKELETONS(u32_or, uint32_t, uint32_t, I_OR)
+DEFINE_SKELETONS(u32_xor, uint32_t, uint32_t, I_XOR)
+DEFINE_SKELETONS(f32_add, float, float, F_ADD)
+DEFINE_SKELETONS(f32_mul, float, float, F_MUL)
+DEFINE_SKELETONS(f32_min, float, float, F_MINf)
+DEFINE_SKELETONS(f32_max, float, float, F_MAXf)
+DEFINE_SKELETONS(f64_add, double, double, F_ADD)
+DEFINE_SKELETONS(f64_mul, double, double, F_MUL)
+DEFINE_SKELETONS(f64_min, double, double, F_MINd)
+DEFINE_SKELETONS(f64_max, double, double, F_MAXd)
+
+/* Dispatch: X(name) expands once per supported (type, op) pair. */
+#define DISPATCH(type, op, CALL)                                              \
+  switch ((type) * 8 + (op)) {                                                \
+    case T_I32 * 8 + O_ADD: CALL(i32_add, int32_t); break;                    \
+    case T_I32 * 8 + O_MUL: CALL(i32_mul, int32_t); break;                    \
+    case T_I32 * 8 + O_MIN: CALL(i32_min, int32_t); break;                    \
+    case T_I32 * 8 + O_MAX: CALL(i32_max, int32_t); break;                    \
+    case T_I32 * 8 + O_AND: CALL(i32_and, int32_t); break;                    \
+    case T_I32 * 8 + O_OR: CALL(i32_or, int32_t); break;                      \
+    case T_I32 * 8 + O_XOR: CALL(i32_xor, int32_t); break;                    \
+    case T_I64 * 8 + O_ADD: CALL(i64_add, int64_t); break;                    \
+    case T_I64 * 8 + O_MUL: CALL(i64_mul, int64_t); break;                    \
+    case T_I64 * 8 + O_MIN: CALL(i64_min, int64_t); break;                    \
+    case T_I64 * 8 + O_MAX: CALL(i64_max, int64_t); break;                    \
+    case T_I64 * 8 + O_AND: CALL(i64_and, int64_t); break;                    \
+    case T_I64 * 8 + O_OR: CALL(i64_or, int64_t); break;                      \
+    case T_I64 * 8 + O_XOR: CALL(i64_xor, int64_t); break;                    \
+    case T_U32 * 8 + O_ADD: CALL(u32_add, uint32_t); break;                   \
+    case T_U32 * 8 + O_MUL: CALL(u32_mul, uint32_t); break;                   \
+    case T_U32 * 8 + O_MIN: CALL(u32_min, uint32_t); break;                   \
+    case T_U32 * 8 + O_MAX: CALL(u32_max, uint32_t); break;                   \
+    case T_U32 * 8 + O_AND: CALL(u32_and, uint32_t); break;                   \
+    case T_U32 * 8 + O_OR: CALL(u32_or, uint32_t); break;                     \
+    case T_U32 * 8 + O_XOR: CALL(u32_xor, uint32_t); break;                   \
+    case T_F32 * 8 + O_ADD: CALL(f32_add, float); break;                      \
+    case T_F32 * 8 + O_MUL: CALL(f32_mul, float); break;                      \
+    case T_F32 * 8 + O_MIN: CALL(f32_min, float); break;                      \
+    case T_F32 * 8 + O_MAX: CALL(f32_max, float); break;                      \
+    case T_F64 * 8 + O_ADD: CALL(f64_add, double); break;                     \
+    case T_F64 * 8 + O_MUL: CALL(f64_mul, double); break;                     \
+    case T_F64 * 8 + O_MIN: CALL(f64_min, double); break;                     \
+    case T_F64 * 8 + O_MAX: CALL(f64_max, double); break;                     \
+    default: return (type < 0 || type > 4 || op < 0 || op > 6) ? E_INVALID : E_UNSUPPORTED; \
+  }
+
+int orc_fold(int op, int type, const void *in, void *out, int64_t outer, int64_t inner, const void *seed, int nth) {
+  if (outer < 0 || inner < 0) return E_INVALID;
+  if (outer == 0) return OK;
+  if (inner == 0 && !seed) return E_EMPTY;
+#define CALL_FOLD(N, T)                                                          \
+  if (inner == 0) { for (int64_t r = 0; r < outer; ++r) ((T *)out)[r] = *(const T *)seed; } \
+  else N##_fold((const T *)in, (T *)out, outer, inner, (const T *)seed, nth)
+  DISPATCH(type, op, CALL_FOLD)
+  return OK;
+}
+
+int orc_fold_seg(int op, int type, const void *in, const void *off, int offtype, void *out, int64_t outer,
+                 int64_t inner, int64_t nseg, const void *seed, int nth) {
+  if (outer < 0 || inner < 0 || nseg < 0 || (offtype != T_I32 && offtype != T_I64)) return E_INVALID;
+  int bad = 0;
+#define CALL_SEG(N, T) N##_foldseg((const T *)in, off, offtype == T_I64, (T *)out, outer, inner, nseg, (const T *)seed, nth, &bad)
+  DISPATCH(type, op, CALL_SEG)
+  return bad ? E_INDEX : OK;
+}
+
+/* kind: 0 inclusive (scanl1/scanr1), 1 seeded (scanl/scanr, n+1 out), 2 prime (scanl'/scanr'). */
+int orc_scan(int op, int type, int dir, int kind, const void *in, void *out, void *sums, int64_t outer,
+             int64_t inner, const void *seed, int nth) {
+  if (outer < 0 || inner < 0 || kind < 0 || kind > 2 || dir < 0 || dir > 1) return E_INVALID;
+  if (kind != 0 && !seed) return E_INVALID;
+#define CALL_SCAN(N, T) N##_scan((const T *)in, (T *)out, (T *)sums, outer, inner, dir, kind, (const T *)seed, nth)
+  DISPATCH(type, op, CALL_SCAN)
+  return OK;
+}
+
+int orc_permute(int op, int type, const void *src, const void *cval, const void *idx, int idxtype, void *out,
+                int64_t n, int64_t m, int nth) {
+  if (n < 0 || m < 0 || (idxtype != T_I32 && idxtype != T_I64) || (!src && !cval)) return E_INVALID;
+  int bad = 0;
+#define CALL_PERM(N, T) N##_permute((const T *)src, (const T *)cval, idx, idxtype == T_I64, (T *)out, n, m, nth, &bad)
+  DISPATCH(type, op, CALL_PERM)
+  return bad ? E_INDEX : OK;
+}
+
+/* ------------------------------------------------------------------ FP64 oracle
+ * Float folds, scans and segmented folds evaluated in FP64 (Neumaier
+ * compensated for +): the reference against which Float32 errors are stated. */
+typedef struct { double s, c; } dd;
+static inline dd dd_add(dd a, double x) {
+  double t = a.s + x;
+  if (fabs(a.s) >= fabs(x)) a.c += (a.s - t) + x; else a.c += (x - t) + a.s;
+  a.s = t;
+  return a;
+}
+static inline double f64_comb(int op, double a, double b) {
+  switch (op) {
+    case O_ADD: return a + b;
+    case O_MUL: return a * b;
+    case O_MIN: return fmin(a, b);
+    default: return fmax(a, b);
+  }
+}
+static inline double ld_f(int type, const void *p, int64_t i) {
+  return type == T_F32 ? (double)((const float *)p)[i] : ((const double *)p)[i];
+}
+
+static double fold_span_f64(int op, int type, const void *in, int64_t u, int64_t v, const double *seed) {
+  if (op == O_ADD) {
+    dd a = {seed ? *seed : 0.0, 0.0};
+    for (int64_t i = u; i < v; ++i) a = dd_add(a, ld_f(type, in, i));
+    return a.s + a.c;
+  }
+  double acc = seed ? *seed : ld_f(type, in, u);
+  for (int64_t i = seed ? u : u + 1; i < v; ++i) acc = f64_comb(op, acc, ld_f(type, in, i));
+  return acc;
+}
+
+int orc_fold_f64(int op, int type, const void *in, double *out, int64_t outer, int64_t inner, const double *seed) {
+  if ((type != T_F32 && type != T_F64) || op > O_MAX) return E_UNSUPPORTED;
+  if (inner == 0 && !seed) return E_EMPTY;
+  _Pragma("omp parallel for schedule(static)")
+  for (int64_t r = 0; r < outer; ++r) out[r] = fold_span_f64(op, type, in, r * inner, r * inner + inner, seed);
+  return OK;
+}
+
+int orc_fold_seg_f64(int op, int type, const void *in, const void *off, int offtype, double *out, int64_t outer,
+                     int64_t inner, int64_t nseg, const double *seed) {
+  if ((type != T_F32 && type != T_F64) || op > O_MAX) return E_UNSUPPORTED;
+  _Pragma("omp parallel for schedule(static)")
+  for (int64_t j = 0; j < outer * nseg; ++j) {
+    int64_t r = j / nseg, s = j % nseg;
+    int64_t u = offtype == T_I64 ? ((const int64_t *)off)[s] : ((const int32_t *)off)[s];
+    int64_t v = offtype == T_I64 ? ((const int64_t *)off)[s + 1] : ((const int32_t *)off)[s + 1];
+    if (u < 0 || v < u || v > inner) continue;
+    if (u == v && !seed) { out[j] = NAN; continue; }
+    out[j] = fold_span_f64(op, type, in, r * inner + u, r * inner + v, seed);
+  }
+  return OK;
+}
+
+/* Inclusive (kind 0) or the same flavours as orc_scan, in FP64. */
+int orc_scan_f64(int op, int type, int dir, int kind, const void *in, double *out, double *sums, int64_t outer,
+                 int64_t inner, const double *seed) {
+  if ((type != T_F32 && type != T_F64) || op > O_MAX) return E_UNSUPPORTED;
+  const int64_t op_ = kind == 1 ? inner + 1 : inner;
+  _Pragma("omp parallel for schedule(static)")
+  for (int64_t r = 0; r < outer; ++r) {
+    const int64_t base = r * inner;
+    double *o = out + r * op_;
+    dd a = {seed ? *seed : 0.0, 0.0};
+    double acc = seed ? *seed : 0.0;
+    int have = seed != 0;
+    const int64_t n = inner;
+    for (int64_t k = 0; k < n; ++k) {
+      const int64_t i = dir ? n - 1 - k : k;
+      const double x = ld_f(type, in, base + i);
+      const int64_t wi = kind == 1 && !dir ? i + 1 : i;
+      if (kind == 2) o[i] = op == O_ADD ? a.s + a.c : acc;
+      if (op == O_ADD) a = dd_add(a, x);
+      else acc = have ? (dir ? f64_comb(op, x, acc) : f64_comb(op, acc, x)) : x;
+      have = 1;
+      if (kind != 2) o[wi] = op == O_ADD ? a.s + a.c : acc;
+    }
+    const double tot = op == O_ADD ? a.s + a.c : acc;
+    if (kind == 1) o[dir ? n : 0] = *seed;
+    if (kind == 2 && sums) sums[r] = tot;
+  }
+  return OK;
+}
+
+/* ------------------------------------------------------------------ stencil */
+static inline int64_t bound_ix(int64_t i, int64_t n, int b) {
+  if (i < 0) { if (b == 0) i = 0; else if (b == 1) i = -i; else if (b == 2) i = n + i; }
+  else if (i >= n) { if (b == 0) i = n - 1; else if (b == 1) i = n - (i - n + 2); else if (b == 2) i = i - n; }
+  return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+
+#define DEFINE_STENCIL(NAME, T, U, MUL, ADD, ID)                                                              \
+  static void NAME##_stencil(int ry, int rx, const T *w, int b, const T *cval, const T *in, int64_t ih,        \
+                             int64_t iw, T *out, int64_t h, int64_t wd, int accumulate, int nth) {       \
+    const int64_t ip = iw, op = wd;                                                                          \
+    _Pragma("omp parallel for schedule(static) if (nth > 1)")                                                \
+    for (int64_t y = 0; y < h; ++y)                                                                          \
+      for (int64_t x = 0; x < wd; ++x) {                                                                     \
+        T acc = accumulate ? out[y * op + x] : (ID);                                                         \
+        for (int dy = -ry; dy <= ry; ++dy)                                                                   \
+          for (int dx = -rx; dx <= rx; ++dx) {                                                               \
+            const T wk = w[(dy + ry) * (2 * rx + 1) + (dx + rx)];                                            \
+            if (wk == 0) continue;                                                                           \
+            const int64_t yy = y + dy, xx = x + dx;                                                          \
+            T v;                                                                                             \
+            if (yy >= 0 && yy < ih && xx >= 0 && xx < iw) v = in[yy * ip + xx];                              \
+            else if (b == 3) v = *cval;                                                                      \
+            else v = in[bound_ix(yy, ih, b) * ip + bound_ix(xx, iw, b)];                                     \
+            acc = ADD(acc, MUL(wk, v));                                                                      \
+          }                                                                                                  \
+        out[y * op + x] = acc;                                                                               \
+      }                                                                                                      \
+  }
+#define S_FMUL(a, b) ((a) * (b))
+#define S_FADD(a, b) ((a) + (b))
+#define S_IMUL32(a, b) ((int32_t)((uint32_t)(a) * (uint32_t)(b)))
+#define S_IADD32(a, b) ((int32_t)((uint32_t)(a) + (uint32_t)(b)))
+#define S_IMUL64(a, b) ((int64_t)((uint64_t)(a) * (uint64_t)(b)))
+#define S_IADD64(a, b) ((int64_t)((uint64_t)(a) + (uint64_t)(b)))
+DEFINE_STENCIL(f32, float, float, S_FMUL, S_FADD, -0.0f)
+DEFINE_STENCIL(f64, double, double, S_FMUL, S_FADD, -0.0)
+DEFINE_STENCIL(i32, int32_t, uint32_t, S_IMUL32, S_IADD32, 0)
+DEFINE_STENCIL(i64, int64_t, uint64_t, S_IMUL64, S_IADD64, 0)
+
+int orc_stencil2d(int type, int ry, int rx, const void *w, int boundary, const void *cval, const void *in, int64_t ih,
+                  int64_t iw, void *out, int64_t h, int64_t wd, int accumulate, int nth) {
+  if (ry < 0 || ry > 4 || rx < 0 || rx > 4 || boundary < 0 || boundary > 3 || h < 0 || wd < 0) return E_INVALID;
+  if (boundary == 3 && !cval) return E_INVALID;
+  switch (type) {
+    case T_F32: f32_stencil(ry, rx, w, boundary, cval, in, ih, iw, out, h, wd, accumulate, nth); break;
+    case T_F64: f64_stencil(ry, rx, w, boundary, cval, in, ih, iw, out, h, wd, accumulate, nth); break;
+    case T_I32: i32_stencil(ry, rx, w, boundary, cval, in, ih, iw, out, h, wd, accumulate, nth); break;
+    case T_I64: i64_stencil(ry, rx, w, boundary, cval, in, ih, iw, out, h, wd, accumulate, nth); break;
+    default: return E_UNSUPPORTED;
+  }
+  return OK;
+}

@@ -1,0 +1,38 @@
+"""Regenerate known_answers.json from the reference's own sources.
+
+The reference ships two known answers for this path, both as text in its
+sources (read here as text; nothing of the reference is executed):
+  * accelerate-llvm-ptx/test/nofib/Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs:
+    `A.sum (A.map (+1) xs)` over xs = [1..n], n = 10000, must equal
+    n * (n + 1) `div` 2 + n (= 50015000);
+  * accelerate-llvm-native/src/Data/Array/Accelerate/LLVM/Native/CodeGen/Scan.hs:
+    the example `scanl (+) 10 (use $ fromList (Z :. 10) [0..])`
+    ==> Array (Z :. 11) [10,10,11,13,16,20,25,31,38,46,55].
+Run:  python tests/golden/make_golden.py [path/to/accelerate-llvm checkout]
+"""
+import json
+import pathlib
+import re
+import sys
+
+ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+runq = (ref / "accelerate-llvm-ptx/test/nofib/Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs").read_text()
+scan = (ref / "accelerate-llvm-native/src/Data/Array/Accelerate/LLVM/Native/CodeGen/Scan.hs").read_text()
+
+assert "A.sum (A.map (+1)" in runq
+n = int(re.search(r"let n = (\d+)", runq).group(1))
+assert "n * (n + 1) `div` 2 + n" in runq
+total = n * (n + 1) // 2 + n
+
+m2 = re.search(r"scanl \(\+\) (\d+) \(use \$ fromList \(Z :\. (\d+)\) \[0\.\.\]\)\s*\n-- >\s*\n-- > ==> Array \(Z :\. (\d+)\) \[([0-9,]+)\]", scan)
+seed, cnt, n_out, vals = int(m2.group(1)), int(m2.group(2)), int(m2.group(3)), [int(v) for v in m2.group(4).split(",")]
+
+golden = {
+    "sum_map_succ": {"source": "accelerate-llvm-ptx/test/nofib/Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs",
+                     "input_range": [1, n], "map": "+1", "op": "+", "seed": 0, "expect": total},
+    "scanl_example": {"source": "accelerate-llvm-native/src/Data/Array/Accelerate/LLVM/Native/CodeGen/Scan.hs",
+                      "op": "+", "seed": seed, "input": list(range(cnt)), "expect": vals, "out_len": n_out},
+}
+out = pathlib.Path(__file__).with_name("known_answers.json")
+out.write_text(json.dumps(golden) + "\n")
+print(out, total, vals)

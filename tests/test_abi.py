@@ -1,0 +1,61 @@
+"""CPU tests of the C ABI: the library loads, exports every entry point the
+header declares, and rejects bad arguments before touching the device."""
+import ctypes
+import pathlib
+import re
+
+import pytest
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "acc_gb300.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__ as ge
+    path = ge._load_build().build()
+    pkg = ge.load_package()
+    return pkg.load(path)
+
+
+def declared():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(acc_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    for n in ["acc_fold", "acc_fold_seg", "acc_scan", "acc_permute", "acc_stencil2d", "acc_sync"]:
+        assert n in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared():
+        assert hasattr(lib, name), name
+
+
+def test_python_signatures_cover_header(lib):
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    assert set(declared()) <= set(pkg.SIGNATURES)
+
+
+def test_version_and_strerror(lib):
+    assert lib.acc_version() == 1
+    assert lib.acc_strerror(0) == b"ok"
+    assert b"empty" in lib.acc_strerror(3)
+    assert lib.acc_strerror(12345) == b"unknown status"
+
+
+def test_argument_validation_without_device(lib):
+    N = None
+    # negative extents, bad enums, missing seeds: rejected before any CUDA call
+    assert lib.acc_fold(0, 0, 0, N, N, -1, 4, N, N) == 1
+    assert lib.acc_fold(0, 0, 0, N, ctypes.c_void_p(16), 2, 0, N, N) == 3  # fold1 of an empty row
+    assert lib.acc_scan(0, 0, 0, 7, 0, N, N, N, 1, 4, N, N) == 1           # bad direction
+    assert lib.acc_scan(0, 0, 0, 0, 1, N, N, N, 1, 4, N, N) == 1           # scanl without seed
+    assert lib.acc_permute(0, 0, N, N, N, 0, N, 4, 4, N) == 1              # no source, no constant
+    assert lib.acc_permute(0, 0, N, N, N, 9, N, 4, 4, N) == 1              # bad index type
+    assert lib.acc_stencil2d(3, 5, 1, N, 0, N, N, N, 4, 4, N) == 1         # radius > 4
+    assert lib.acc_stencil2d(2, 1, 1, N, 0, N, N, N, 4, 4, N) == 2         # Word32 stencil unsupported
+    assert lib.acc_fold_seg(0, 0, 0, N, N, 3, N, 1, 4, 2, N, N) == 1       # bad offset type

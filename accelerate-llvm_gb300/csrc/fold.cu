@@ -181,7 +181,7 @@ int fold_typed(Workspace *w, const T *in, T *out, int64_t outer, int64_t inner, 
   const int64_t row_bytes = inner * (int64_t)sizeof(T);
   // Enough rows to fill the machine with one warp each, and rows short
   // enough that one warp streams them quickly: a warp per row.
-  if (row_bytes <= (64 << 10) && outer >= (int64_t)d.sms * 32) {
+  if (row_bytes <= (32 << 10) && outer >= (int64_t)d.sms * 8) {
     int64_t blocks = cdiv_h(outer, 8);
     if (blocks > (int64_t)d.sms * 32) blocks = (int64_t)d.sms * 32;
     fold_rows_warp<OP, T, PREC><<<(unsigned)blocks, 256, 0, s>>>(fa);

@@ -36,6 +36,7 @@ struct SegArgs {
   uint32_t *nlong;     // number of listed long segments
   int64_t *longs;      // listed long segment ids
   int64_t long_ctas;   // CTAs [0, long_ctas) work on the list
+  int64_t long_cap;    // capacity of the list
   uint32_t *err;
 };
 
@@ -48,6 +49,9 @@ __global__ void seg_classify(SegArgs a) {
     const int64_t u = seg_off(a, s), v = seg_off(a, s + 1);
     if (v - u > LONG_SEG && u >= 0 && v <= a.inner) {
       const uint32_t k = atomicAdd(a.nlong, 1u);
+      // Valid offsets give at most inner / LONG_SEG long segments; overlapping
+      // (malformed) offsets could give more: never write past the list.
+      if ((int64_t)k >= a.long_cap) { raise_error(a.err, DEV_ERR_INDEX); continue; }
       a.longs[k] = s;
     }
   }
@@ -101,7 +105,8 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
 
   if ((int64_t)blockIdx.x < a.long_ctas) {
     // ---- long segments: one CTA per (row, listed segment)
-    const int64_t nl = (int64_t)ld_relaxed_u32(a.nlong);
+    int64_t nl = (int64_t)ld_relaxed_u32(a.nlong);
+    if (nl > a.long_cap) nl = a.long_cap;
     for (int64_t job = blockIdx.x; job < nl * a.outer; job += a.long_ctas) {
       const int64_t r = job / nl, s = a.longs[job % nl];
       const int64_t u = seg_off(a, s), v = seg_off(a, s + 1);
@@ -183,6 +188,7 @@ int foldseg_typed(Workspace *w, const T *in, const void *off, int off64, T *out,
   a.seed = seed; a.has_seed = has_seed;
   a.nlong = w->words + W_SEGBIG;
   a.longs = static_cast<int64_t *>(w->scratch);
+  a.long_cap = maxlong;
   a.err = w->words + W_ERR;
   // Only a row longer than LONG_SEG can hold a long segment.
   a.long_ctas = 0;

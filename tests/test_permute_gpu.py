@@ -28,7 +28,7 @@ def run_perm(acc, orc, dev, t, op, n, m, const=False, idx_t=np.int32, drop=True)
     acc.sync()
     got = got.cpu().numpy()
     ref = orc.permute(op, defaults, idx, xs, cval=c)
-    if np.dtype(dt).kind in "iu" or op in ("min", "max"):
+    if np.dtype(dt).kind in "iu" or op in ("min", "max", "*"):
         same = (got == ref) | (np.isnan(got.astype(np.float64)) & np.isnan(ref.astype(np.float64)))
         assert same.all(), _diff(got, ref)
     else:

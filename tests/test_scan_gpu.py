@@ -26,7 +26,7 @@ def check_scan(orc, got, xs, dt, op, z, d, k):
         ref_out, ref_sum = ref
     else:
         got_out, ref_out = got, ref
-    if dt.kind in "iu" or op in ("min", "max"):
+    if dt.kind in "iu" or op in ("min", "max", "*"):
         assert np.array_equal(got_out, ref_out) or (dt.kind == "f" and _nan_equal(got_out, ref_out)), _diff(got_out, ref_out)
         if k == 2:
             assert np.array_equal(got_sum, ref_sum) or _nan_equal(got_sum, ref_sum)

@@ -25,12 +25,18 @@
 // Rows of a rank >= 2 array are scanned by scan_rows_kernel: one CTA per row
 // with a carried prefix, as the reference's `scan` (multi-dim) kernel does
 // (PTX/CodeGen/Scan.hs:746-939).
+#include <cstdlib>
+#include <cstring>
+
 #include "common.cuh"
 
 namespace accgb {
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ROW_BYTES = 128;  // one thread row = one 128 B swizzle line
+#ifndef SCAN_LOOKBACK
+#define SCAN_LOOKBACK 4  // predecessor statuses read per lane per look-back round trip
+#endif
 
 struct ScanArgs {
   const void *in;
@@ -82,158 +88,144 @@ __device__ __forceinline__ uint32_t peek(const uint64_t *status, int64_t t, uint
   return tag & 3u;
 }
 
-template <int OP, class T, int PREC, bool R2L>
-__global__ void __launch_bounds__(SCAN_THREADS)
-scan_lookback_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+// One tile = SUB sub-tiles of 256 rows x 128 B; thread t owns row t of every
+// sub-tile.  The rows of the array's full 128 B lines are in `buf` (each
+// sub-tile 32 KiB, 128-byte swizzled); the last, partial line is read from
+// and written to global memory directly.  The row is NOT kept in registers
+// across the look-back: pass 1 folds it, pass 2 re-reads it from shared memory
+// and rescans it from its prefix, which keeps the register count low enough
+// for many tiles per SM to be in flight.  On return the results of the full
+// rows are in `buf`.
+template <int OP, class T, int PREC, bool R2L, int SUB>
+__device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile, const ScanArgs &a,
+                                               typename Acc<OP, T, PREC>::S (*s_warp)[SCAN_THREADS / 32],
+                                               typename Acc<OP, T, PREC>::S &s_prefix, bool smem_all_rows) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
   constexpr int VEC = 16 / sizeof(T);
-  constexpr int TILE = SCAN_THREADS * ITEMS;
   constexpr int NWARP = SCAN_THREADS / 32;
-
-  extern __shared__ unsigned char smem_raw[];
-  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t bar;
-  __shared__ int64_t s_tile;
-  __shared__ S s_warp[NWARP];
-  __shared__ S s_prefix;
-
+  constexpr int SUB_BYTES = SCAN_THREADS * SCAN_ROW_BYTES;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-  if (tid == 0) {
-    uint32_t dyn = atomicAdd(a.ticket, 1u);
-    // The holder of the last ticket knows every other CTA has taken its
-    // ticket: it re-arms the counter for the next launch on this stream.
-    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
-    s_tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
-    if (a.tma_in) {
-      mbar_init(&bar, 1);
-      fence_mbar_init();
-    }
-  }
-  __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t row0 = tile * SCAN_THREADS;  // first 128 B row of the tile
   const T idT = Prim<OP, T>::id();
+  const int64_t row0 = tile * (int64_t)(SUB * SCAN_THREADS);
 
-  // ---------------------------------------------------------------- load
-  if (a.tma_in) {
-    if (tid == 0) {
-      prefetch_tmap(&tin);
-      mbar_expect_tx(&bar, TILE * sizeof(T));
-      tma_load_2d(buf, &tin, 0, (int)row0, &bar);
+  auto load_row = [&](int u, T (&x)[ITEMS]) {
+    const int64_t grow = row0 + u * SCAN_THREADS + tid;
+    if (smem_all_rows || grow < a.full_rows) {
+#pragma unroll
+      for (int c = 0; c < ITEMS / VEC; ++c) {
+        uint4 v = *reinterpret_cast<const uint4 *>(buf + u * SUB_BYTES + swz(tid, c));
+        memcpy(&x[c * VEC], &v, 16);
+      }
+    } else {
+      const T *src = static_cast<const T *>(a.in);
+      const int64_t e0 = grow * ITEMS;
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
     }
-    if (!mbar_wait(&bar, 0)) {
-      raise_error(a.err, DEV_ERR_TIMEOUT);
-      mbar_wait(&bar, 0);  // the copy is ours: give it a second bounded chance to land
-    }
-  } else {
-    // Coalesced loads into the same swizzled layout the TMA would produce.
-    const T *src = static_cast<const T *>(a.in);
-    const int64_t base = tile * (int64_t)TILE;
-    for (int e = tid; e < TILE; e += SCAN_THREADS) {
-      int64_t gi = base + e;
-      T v = gi < a.n ? src[gi] : idT;
-      int r = e / ITEMS, k = e % ITEMS;
-      *reinterpret_cast<T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T)) = v;
-    }
-    __syncthreads();
-  }
+  };
 
-  const int64_t myrow = row0 + tid;
-  const int64_t e0 = myrow * ITEMS;
-  T x[ITEMS];
-  const bool from_smem = !a.tma_in || myrow < a.full_rows;
-  if (from_smem) {
+  // ---- pass 1: row totals, warp scans, warp totals
+  S excl_lane[SUB];
 #pragma unroll
-    for (int c = 0; c < ITEMS / VEC; ++c) {
-      uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(tid, c));
-      memcpy(&x[c * VEC], &v, 16);
+  for (int u = 0; u < SUB; ++u) {
+    T x[ITEMS];
+    load_row(u, x);
+    S agg;
+    if (!R2L) {
+      agg = A::lift(x[0]);
+#pragma unroll
+      for (int j = 1; j < ITEMS; ++j) agg = A::push(agg, x[j]);
+      S incl = warp_scan_incl<A>(agg);
+      S up = shfl_up(incl, 1);
+      excl_lane[u] = lane == 0 ? A::id() : up;
+      if (lane == 31) s_warp[u][warp] = incl;
+    } else {
+      agg = A::lift(x[ITEMS - 1]);
+#pragma unroll
+      for (int j = ITEMS - 2; j >= 0; --j) agg = A::push(agg, x[j]);
+      S incl = warp_scan_incl_rev<A>(agg);
+      S dn = shfl_down(incl, 1);
+      excl_lane[u] = lane == 31 ? A::id() : dn;
+      if (lane == 0) s_warp[u][warp] = incl;
     }
-  } else {
-    const T *src = static_cast<const T *>(a.in);
-#pragma unroll
-    for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
-  }
-
-  // ---------------------------------------------------------------- reduce
-  S agg;
-  if (!R2L) {
-    agg = A::lift(x[0]);
-#pragma unroll
-    for (int j = 1; j < ITEMS; ++j) agg = A::push(agg, x[j]);
-  } else {
-    agg = A::lift(x[ITEMS - 1]);
-#pragma unroll
-    for (int j = ITEMS - 2; j >= 0; --j) agg = A::push(agg, x[j]);
-  }
-
-  S incl, excl_lane;
-  if (!R2L) {
-    incl = warp_scan_incl<A>(agg);
-    S up = shfl_up(incl, 1);
-    excl_lane = lane == 0 ? A::id() : up;
-    if (lane == 31) s_warp[warp] = incl;
-  } else {
-    incl = warp_scan_incl_rev<A>(agg);
-    S dn = shfl_down(incl, 1);
-    excl_lane = lane == 31 ? A::id() : dn;
-    if (lane == 0) s_warp[warp] = incl;
   }
   __syncthreads();
 
-  S wpre = A::id();
-  if (!R2L) {
-    for (int w = 0; w < warp; ++w) wpre = A::comb(wpre, s_warp[w]);
-  } else {
-    for (int w = warp + 1; w < NWARP; ++w) wpre = A::comb(wpre, s_warp[w]);
-  }
-
-  // ---------------------------------------------------------------- look-back
+  // ---- decoupled look-back (warp 0)
   if (warp == 0) {
-    S bagg = s_warp[0];
+    S bagg = s_warp[0][0];
 #pragma unroll
-    for (int w = 1; w < NWARP; ++w) bagg = A::comb(bagg, s_warp[w]);
+    for (int k = 1; k < SUB * NWARP; ++k) bagg = A::comb(bagg, s_warp[k / NWARP][k % NWARP]);
     const bool first = R2L ? (tile == a.ntiles - 1) : (tile == 0);
     S prefix;
     if (first) {
       prefix = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
     } else {
       if (lane == 0) publish<S>(a.status, tile, a.epoch, 1u, bagg);
+      // Each lane inspects LB consecutive predecessors per round trip, so one
+      // window covers 32 * LB tiles.
+      constexpr int LB = SCAN_LOOKBACK;
       S acc = A::id();
       int64_t k0 = 0;
       bool gave_up = false;
       while (true) {
-        const int64_t pt = R2L ? tile + 1 + k0 + lane : tile - 1 - k0 - lane;
-        const bool exists = R2L ? (pt < a.ntiles) : (pt >= 0);
-        uint32_t flag = exists ? 0u : 2u;
-        S v = A::id();
+        uint32_t fl[LB];
+        S v[LB];
+        bool ex[LB];
+#pragma unroll
+        for (int i = 0; i < LB; ++i) {
+          const int64_t d = k0 + lane * LB + i;  // 0 = nearest predecessor
+          const int64_t pt = R2L ? tile + 1 + d : tile - 1 - d;
+          ex[i] = R2L ? (pt < a.ntiles) : (pt >= 0);
+          fl[i] = ex[i] ? 0u : 2u;
+          v[i] = A::id();
+        }
         uint32_t it = 0;
         while (true) {
-          if (exists && flag == 0) flag = peek<S>(a.status, pt, a.epoch, v);
-          if (__all_sync(0xffffffffu, flag != 0)) break;
+          bool ready = true;
+#pragma unroll
+          for (int i = 0; i < LB; ++i) {
+            if (ex[i] && fl[i] == 0) {
+              const int64_t d = k0 + lane * LB + i;
+              fl[i] = peek<S>(a.status, R2L ? tile + 1 + d : tile - 1 - d, a.epoch, v[i]);
+            }
+            ready = ready && fl[i] != 0;
+          }
+          if (__all_sync(0xffffffffu, ready)) break;
           ++it;
           // Give up (warp-uniformly) after SPIN_LIMIT polls, or at once when
           // another CTA on this stream has already timed out.
-          bool stop = gave_up || it > SPIN_LIMIT ||
-                      ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
+          const bool stop = gave_up || it > SPIN_LIMIT ||
+                            ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
           if (__any_sync(0xffffffffu, stop)) {
             gave_up = true;
             if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
-            if (flag == 0) flag = 2u;  // treat as identity: the result is flagged as failed
+#pragma unroll
+            for (int i = 0; i < LB; ++i)
+              if (fl[i] == 0) fl[i] = 2u;  // treat as identity: the result is flagged as failed
             break;
           }
           __nanosleep(it < 8 ? 32 : 128);
         }
-        const unsigned pmask = __ballot_sync(0xffffffffu, flag == 2u);
+        // Lane-local fold from the nearest predecessor outwards, up to and
+        // including the first inclusive prefix.
+        bool seen_p = false;
+        S lv = A::id();
+#pragma unroll
+        for (int i = 0; i < LB; ++i) {
+          if (!seen_p) lv = R2L ? A::comb(lv, v[i]) : A::comb(v[i], lv);
+          seen_p = seen_p || fl[i] == 2u;
+        }
+        const unsigned pmask = __ballot_sync(0xffffffffu, seen_p);
         const int kp = pmask ? __ffs(pmask) - 1 : 32;
-        if (lane > kp) v = A::id();
-        S wv = R2L ? warp_reduce<A>(v) : warp_reduce_rev<A>(v);
+        if (lane > kp) lv = A::id();
+        S wv = R2L ? warp_reduce<A>(lv) : warp_reduce_rev<A>(lv);
         wv = shfl_idx(wv, 0);
         acc = R2L ? A::comb(acc, wv) : A::comb(wv, acc);
         if (pmask) break;
-        k0 += 32;
+        k0 += 32 * LB;
       }
       prefix = acc;
     }
@@ -248,61 +240,134 @@ scan_lookback_kernel(const __grid_constant__ CUtensorMap tin, const __grid_const
   }
   __syncthreads();
 
-  // ---------------------------------------------------------------- rescan + store
-  S run = R2L ? A::comb(A::comb(excl_lane, wpre), s_prefix) : A::comb(s_prefix, A::comb(wpre, excl_lane));
-  T y[ITEMS];
-  if (!R2L) {
+  // ---- pass 2: rescan each row from its prefix, results back to buf / global
+  T *dst = static_cast<T *>(a.out);
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      if (a.exclusive) { y[j] = A::lower(run); run = A::push(run, x[j]); }
-      else { run = A::push(run, x[j]); y[j] = A::lower(run); }
+  for (int u = 0; u < SUB; ++u) {
+    // Everything before (L2R) / after (R2L) this thread's row within the tile.
+    S inner = A::id();
+    if (!R2L) {
+      for (int k = 0; k < u * NWARP + warp; ++k) inner = A::comb(inner, s_warp[k / NWARP][k % NWARP]);
+    } else {
+      for (int k = u * NWARP + warp + 1; k < SUB * NWARP; ++k) inner = A::comb(inner, s_warp[k / NWARP][k % NWARP]);
     }
-  } else {
+    S run = R2L ? A::comb(A::comb(excl_lane[u], inner), s_prefix) : A::comb(s_prefix, A::comb(inner, excl_lane[u]));
+    T x[ITEMS];
+    load_row(u, x);
+    const int64_t grow = row0 + u * SCAN_THREADS + tid;
+    const bool in_smem = smem_all_rows || grow < a.full_rows;
+    const int64_t e0 = grow * ITEMS;
 #pragma unroll
-    for (int j = ITEMS - 1; j >= 0; --j) {
-      if (a.exclusive) { y[j] = A::lower(run); run = A::push(run, x[j]); }
-      else { run = A::push(run, x[j]); y[j] = A::lower(run); }
+    for (int cc = 0; cc < ITEMS / VEC; ++cc) {
+      const int c = R2L ? ITEMS / VEC - 1 - cc : cc;
+      T y[VEC];
+#pragma unroll
+      for (int kk = 0; kk < VEC; ++kk) {
+        const int k = R2L ? VEC - 1 - kk : kk;
+        const int j = c * VEC + k;
+        if (a.exclusive) { y[k] = A::lower(run); run = A::push(run, x[j]); }
+        else { run = A::push(run, x[j]); y[k] = A::lower(run); }
+      }
+      if (in_smem) {
+        uint4 v;
+        memcpy(&v, y, 16);
+        *reinterpret_cast<uint4 *>(buf + u * SUB_BYTES + swz(tid, c)) = v;
+      } else {
+#pragma unroll
+        for (int k = 0; k < VEC; ++k)
+          if (e0 + c * VEC + k < a.n) dst[e0 + c * VEC + k] = y[k];
+      }
     }
   }
+}
 
+// One tile per CTA, any alignment: coalesced loads / stores through the same
+// swizzled smem layout (used when a TMA descriptor cannot describe the array).
+template <int OP, class T, int PREC, bool R2L>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(ScanArgs a) {
+  using S = typename Acc<OP, T, PREC>::S;
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int TILE = SCAN_THREADS * ITEMS;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ int64_t s_tile;
+  __shared__ S s_warp[1][SCAN_THREADS / 32];
+  __shared__ S s_prefix;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const uint32_t dyn = atomicAdd(a.ticket, 1u);
+    // The holder of the last ticket knows every other CTA has taken its
+    // ticket: it re-arms the counter for the next launch on this stream.
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    s_tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t base = tile * (int64_t)TILE;
+  const T idT = Prim<OP, T>::id();
+  const T *src = static_cast<const T *>(a.in);
+  for (int e = tid; e < TILE; e += SCAN_THREADS) {
+    const int64_t gi = base + e;
+    const T v = gi < a.n ? src[gi] : idT;
+    const int r = e / ITEMS, k = e % ITEMS;
+    *reinterpret_cast<T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T)) = v;
+  }
+  __syncthreads();
+  scan_tile_body<OP, T, PREC, R2L, 1>(buf, tile, a, s_warp, s_prefix, true);
+  __syncthreads();
   T *dst = static_cast<T *>(a.out);
-  if (a.tma_out) {
-    if (myrow < a.full_rows) {
+  for (int e = tid; e < TILE; e += SCAN_THREADS) {
+    const int64_t gi = base + e;
+    if (gi < a.n) {
+      const int r = e / ITEMS, k = e % ITEMS;
+      dst[gi] = *reinterpret_cast<const T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T));
+    }
+  }
+}
+
+// One tile (SUB x 32 KiB) per CTA through TMA, for 16-byte aligned arrays:
+// the tile arrives with SUB 2-D TMA loads of [256 rows x 128 B] on one
+// mbarrier, is scanned in shared memory, and leaves with SUB TMA stores.
+template <int OP, class T, int PREC, bool R2L, int SUB>
+__global__ void __launch_bounds__(SCAN_THREADS, SUB == 1 ? 6 : 3)
+scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+  using S = typename Acc<OP, T, PREC>::S;
+  constexpr int SUB_BYTES = SCAN_THREADS * SCAN_ROW_BYTES;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t bar;
+  __shared__ int64_t s_tile;
+  __shared__ S s_warp[SUB][SCAN_THREADS / 32];
+  __shared__ S s_prefix;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const uint32_t dyn = atomicAdd(a.ticket, 1u);
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    const int64_t tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
+    s_tile = tile;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_expect_tx(&bar, SUB * SUB_BYTES);
 #pragma unroll
-      for (int c = 0; c < ITEMS / VEC; ++c) {
-        uint4 v;
-        memcpy(&v, &y[c * VEC], 16);
-        *reinterpret_cast<uint4 *>(buf + swz(tid, c)) = v;
-      }
-    } else {
+    for (int u = 0; u < SUB; ++u)
+      tma_load_2d(buf + u * SUB_BYTES, &tin, 0, (int)((tile * SUB + u) * SCAN_THREADS), &bar);
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  if (!mbar_wait(&bar, 0)) {
+    raise_error(a.err, DEV_ERR_TIMEOUT);
+    mbar_wait(&bar, 0);
+  }
+  scan_tile_body<OP, T, PREC, R2L, SUB>(buf, tile, a, s_warp, s_prefix, false);
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (tid == 0) {
 #pragma unroll
-      for (int j = 0; j < ITEMS; ++j)
-        if (e0 + j < a.n) dst[e0 + j] = y[j];
-    }
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tma_store_2d(&tout, 0, (int)row0, buf);
-      tma_store_commit();
-      tma_store_wait_read();
-    }
-  } else {
-    __syncthreads();  // every thread has finished reading its row
-#pragma unroll
-    for (int c = 0; c < ITEMS / VEC; ++c) {
-      uint4 v;
-      memcpy(&v, &y[c * VEC], 16);
-      *reinterpret_cast<uint4 *>(buf + swz(tid, c)) = v;
-    }
-    __syncthreads();
-    const int64_t base = tile * (int64_t)TILE;
-    for (int e = tid; e < TILE; e += SCAN_THREADS) {
-      int64_t gi = base + e;
-      if (gi < a.n) {
-        int r = e / ITEMS, k = e % ITEMS;
-        dst[gi] = *reinterpret_cast<const T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T));
-      }
-    }
+    for (int u = 0; u < SUB; ++u)
+      tma_store_2d(&tout, 0, (int)((tile * SUB + u) * SCAN_THREADS), buf + u * SUB_BYTES);
+    tma_store_commit();
+    tma_store_wait_read();
   }
 }
 
@@ -422,19 +487,27 @@ template int launch_fill<double>(double *, int64_t, uint64_t, cudaStream_t);
 // ----------------------------------------------------------------- host side
 constexpr size_t SCAN_SMEM = SCAN_THREADS * SCAN_ROW_BYTES + 1024;
 
-template <int OP, class T, int PREC, bool R2L>
-int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
-                   bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+template <int OP, class T, int PREC, bool R2L, int SUB>
+int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
+                       bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
-  constexpr int64_t TILE = (int64_t)SCAN_THREADS * ITEMS;
-  const int64_t ntiles = cdiv_h(n, TILE);
+  CUtensorMap tin, tout;
+  memset(&tin, 0, sizeof(tin));
+  memset(&tout, 0, sizeof(tout));
+  const int64_t full_rows = n / ITEMS;
+  const bool tma = full_rows > 0 &&
+                   encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true) &&
+                   encode_2d(&tout, out, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
+  const int sub = tma ? SUB : 1;
+  const int64_t tile_elems = (int64_t)sub * SCAN_THREADS * ITEMS;
+  const int64_t ntiles = cdiv_h(n, tile_elems);
   if (ntiles >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
   int st = ws_status(w, (size_t)ntiles * 2);
   if (st) return st;
   ScanArgs a{};
   a.in = in; a.out = out; a.total_out = total_out; a.seed_out = seed_out;
   a.n = n;
-  a.full_rows = n / ITEMS;
+  a.full_rows = full_rows;
   a.ntiles = ntiles;
   a.seed = seed;
   a.status = w->status;
@@ -443,19 +516,40 @@ int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   a.epoch = ws_next_epoch(w, s);
   a.has_seed = has_seed;
   a.exclusive = exclusive;
-  CUtensorMap tin, tout;
-  memset(&tin, 0, sizeof(tin));
-  memset(&tout, 0, sizeof(tout));
-  a.tma_in = a.full_rows > 0 && encode_2d(&tin, in, sizeof(T), ITEMS, a.full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
-  a.tma_out = a.full_rows > 0 && encode_2d(&tout, out, sizeof(T), ITEMS, a.full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
+  a.tma_in = a.tma_out = tma;
+  if (tma) {
+    const size_t smem = (size_t)SUB * SCAN_THREADS * SCAN_ROW_BYTES + 1024;
+    auto kern = scan_tma_kernel<OP, T, PREC, R2L, SUB>;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      attr = true;
+    }
+    kern<<<(unsigned)ntiles, SCAN_THREADS, smem, s>>>(tin, tout, a);
+    return check_launch();
+  }
   auto kern = scan_lookback_kernel<OP, T, PREC, R2L>;
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SCAN_SMEM);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     attr_set = true;
   }
-  kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(tin, tout, a);
+  kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(a);
   return check_launch();
+}
+
+// Tile size: 2 sub-tiles (64 KiB, 3 CTAs per SM) by default, the faster of
+// the two on GB300 at 2^25..2^28 elements; ACC_GB300_SCAN_SUB=1 selects 32 KiB
+// tiles (6 CTAs per SM).
+template <int OP, class T, int PREC, bool R2L>
+int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
+                   bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+  static const int sub = getenv("ACC_GB300_SCAN_SUB") ? atoi(getenv("ACC_GB300_SCAN_SUB")) : 2;
+  if (sub == 2)
+    return launch_scan_1d_sub<OP, T, PREC, R2L, 2>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
+  return launch_scan_1d_sub<OP, T, PREC, R2L, 1>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
 }
 
 template <int OP, class T, int PREC, bool R2L>

@@ -212,8 +212,9 @@ int acc_permute_clone(int op, int type, const void *defaults, const void *src,
  * weighted-sum stencil function:
  *     out[y][x] = sum_{dy=-ry..ry, dx=-rx..rx} w[(dy+ry)*(2rx+1)+(dx+rx)] * in[y+dy][x+dx]
  * accumulated in that tap order (rows outer, -r..r, as the reference's
- * stencil access, accelerate-llvm/.../CodeGen/Stencil.hs:73-180), without
- * fused multiply-add, starting from w[0]*x[0].  Out-of-range reads follow
+ * stencil access, accelerate-llvm/.../CodeGen/Stencil.hs:73-180), one fused
+ * multiply-add per tap (acc = fma(w, x, acc), a single rounding, from
+ * acc = -0.0) for the float types; taps whose weight is zero are skipped.  Out-of-range reads follow
  * `boundary` (CodeGen/Stencil.hs:207-253); `cval` (host pointer) is the
  * constant of ACC_CONSTANT.  Types ACC_F32 / ACC_F64 (float weights) and
  * ACC_I32 / ACC_I64 (integer weights, wrapping).  rx, ry in [0, 4]

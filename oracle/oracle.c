@@ -15,7 +15,8 @@
  *    Instruction.hs:429-473, no nsw/nuw); integer min/max select on <= / >=,
  *    float min/max are fmin/fmax (accelerate-llvm/src/Data/Array/Accelerate/
  *    LLVM/CodeGen/Arithmetic.hs:456-466); no fast-math, no FMA contraction
- *    (this file must be compiled with -ffp-contract=off).
+ *    (this file must be compiled with -ffp-contract=off; the stencil's fused
+ *    multiply-adds are explicit fma() calls).
  *  - fold / fold1: left fold from the seed, z `f` x0 `f` x1 ...
  *    (accelerate-llvm-native/src/Data/Array/Accelerate/LLVM/Native/CodeGen/
  *    Fold.hs:74-100, reduceFromTo / reduce1FromTo :248-275).  A parallel
@@ -34,8 +35,9 @@
  *  - stencil: taps rows outer, -r..r (accelerate-llvm/.../CodeGen/
  *    Stencil.hs:73-180); boundaries clamp / mirror / wrap / constant
  *    (CodeGen/Stencil.hs:195-253).  The stencil function is a weighted sum
- *    accumulated from the additive identity in tap order, multiply and add
- *    rounded separately; zero-weight taps are not part of the pattern.
+ *    accumulated from the additive identity in tap order, one fused
+ *    multiply-add per tap (C99 fma); zero-weight taps are not part of the
+ *    pattern.
  *
  * Besides the restatement in the element type, *_f64 variants compute float
  * folds / scans / segmented folds in FP64 with Neumaier compensation: the
@@ -483,7 +485,7 @@ static inline int64_t bound_ix(int64_t i, int64_t n, int b) {
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
 
-#define DEFINE_STENCIL(NAME, T, U, MUL, ADD, ID)                                                              \
+#define DEFINE_STENCIL(NAME, T, U, TAP, ID)                                                              \
   static void NAME##_stencil(int ry, int rx, const T *w, int b, const T *cval, const T *in, int64_t ih,        \
                              int64_t iw, T *out, int64_t h, int64_t wd, int accumulate, int nth) {       \
     const int64_t ip = iw, op = wd;                                                                          \
@@ -500,21 +502,20 @@ static inline int64_t bound_ix(int64_t i, int64_t n, int b) {
             if (yy >= 0 && yy < ih && xx >= 0 && xx < iw) v = in[yy * ip + xx];                              \
             else if (b == 3) v = *cval;                                                                      \
             else v = in[bound_ix(yy, ih, b) * ip + bound_ix(xx, iw, b)];                                     \
-            acc = ADD(acc, MUL(wk, v));                                                                      \
+            acc = TAP(wk, v, acc);                                                                           \
           }                                                                                                  \
         out[y * op + x] = acc;                                                                               \
       }                                                                                                      \
   }
-#define S_FMUL(a, b) ((a) * (b))
-#define S_FADD(a, b) ((a) + (b))
-#define S_IMUL32(a, b) ((int32_t)((uint32_t)(a) * (uint32_t)(b)))
-#define S_IADD32(a, b) ((int32_t)((uint32_t)(a) + (uint32_t)(b)))
-#define S_IMUL64(a, b) ((int64_t)((uint64_t)(a) * (uint64_t)(b)))
-#define S_IADD64(a, b) ((int64_t)((uint64_t)(a) + (uint64_t)(b)))
-DEFINE_STENCIL(f32, float, float, S_FMUL, S_FADD, -0.0f)
-DEFINE_STENCIL(f64, double, double, S_FMUL, S_FADD, -0.0)
-DEFINE_STENCIL(i32, int32_t, uint32_t, S_IMUL32, S_IADD32, 0)
-DEFINE_STENCIL(i64, int64_t, uint64_t, S_IMUL64, S_IADD64, 0)
+/* One tap, acc + w*x: C99 fma (one rounding) for floats, wrapping for ints. */
+#define T_F32(w, x, acc) fmaf((w), (x), (acc))
+#define T_F64(w, x, acc) fma((w), (x), (acc))
+#define T_I32(w, x, acc) ((int32_t)((uint32_t)(acc) + (uint32_t)(w) * (uint32_t)(x)))
+#define T_I64(w, x, acc) ((int64_t)((uint64_t)(acc) + (uint64_t)(w) * (uint64_t)(x)))
+DEFINE_STENCIL(f32, float, float, T_F32, -0.0f)
+DEFINE_STENCIL(f64, double, double, T_F64, -0.0)
+DEFINE_STENCIL(i32, int32_t, uint32_t, T_I32, 0)
+DEFINE_STENCIL(i64, int64_t, uint64_t, T_I64, 0)
 
 int orc_stencil2d(int type, int ry, int rx, const void *w, int boundary, const void *cval, const void *in, int64_t ih,
                   int64_t iw, void *out, int64_t h, int64_t wd, int accumulate, int nth) {

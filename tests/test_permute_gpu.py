@@ -87,3 +87,18 @@ def test_permute_out_of_range_raises(acc, dev):
 def test_permute_empty(acc, dev):
     out = acc.permute("+", torch.arange(5, dtype=torch.int32, device=dev), torch.empty(0, dtype=torch.int32, device=dev), 1)
     assert out.cpu().tolist() == [0, 1, 2, 3, 4]
+
+
+@pytest.mark.parametrize("c", [1, 7, 2047])
+def test_permute_histogram_counter_wrap(acc, orc, dev, c):
+    # Two adjacent hot bins (one packed word) take most of 2^25 updates, so the
+    # per-CTA 16-bit counters wrap many times, concurrently with the carries.
+    rng = np.random.default_rng(c)
+    n, m = 1 << 25, 1 << 16
+    idx = rng.integers(0, m, size=n).astype(np.int32)
+    hot = rng.random(n) < 0.9
+    idx[hot] = rng.integers(0, 2, size=int(hot.sum())).astype(np.int32) + 2
+    got = acc.permute("+", torch.zeros(m, dtype=torch.int32, device=dev), torch.from_numpy(idx).to(dev), c)
+    acc.sync()
+    ref = (np.bincount(idx, minlength=m).astype(np.int64) * c).astype(np.uint32).view(np.int32)
+    assert np.array_equal(got.cpu().numpy(), ref)

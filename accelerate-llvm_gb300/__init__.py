@@ -78,6 +78,7 @@ SIGNATURES = {
     "acc_fold_seg": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_fold_seg_lengths": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_scan": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
+    "acc_scan_noalloc": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_permute": ([_I, _I, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_permute_clone": ([_I, _I, _P, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_stencil2d": ([_I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _P], _I),

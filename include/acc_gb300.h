@@ -182,6 +182,25 @@ int acc_scan(int op, int type, int prec, int dir, int kind, const void *in,
              void *out, void *sums, int64_t outer, int64_t inner,
              const void *seed, void *stream);
 
+/* acc_scan without any device allocation -- no counterpart in the reference,
+ * which always allocates its temporaries (PTX/Execute.hs:453).  Same
+ * arguments, results and errors as acc_scan, for callers that cannot let a
+ * library call cudaMalloc: a host capturing the stream into a CUDA graph, an
+ * integration with a fixed device-memory budget or its own pool allocator.
+ * The look-back scratch lives in one file-scope device array of 2 MiB (plus
+ * 256 bytes) that every GPU loading the library holds until the process
+ * exits, so a row may have at most 2^28 elements; longer rows return
+ * ACC_ERR_TOO_LARGE before anything is launched.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress): make that first
+ * call before any stream capture.  Every call reuses the same array, so calls
+ * whose work overlaps on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller.  A look-back wait that runs out is not
+ * reported by this entry point (acc_sync reports only acc_scan's workspaces);
+ * the wait is bounded, so the call always completes. */
+int acc_scan_noalloc(int op, int type, int prec, int dir, int kind,
+                     const void *in, void *out, void *sums, int64_t outer,
+                     int64_t inner, const void *seed, void *stream);
+
 /* ---------------------------------------------------------------- permute */
 
 /* permute f defaults p xs, for the fixed primitives.  Replaces permuteOp +

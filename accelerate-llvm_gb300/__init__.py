@@ -83,6 +83,13 @@ SIGNATURES = {
     "acc_permute_clone": ([_I, _I, _P, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_stencil2d": ([_I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _P], _I),
     "acc_stencil2d_pair": ([_I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _L, _L, _P, _L, _L, _P, _P], _I),
+    "acc_batch_create": ([_I, _P, _L, _P], _I),
+    "acc_batch_capture": ([_P, _P], _I),
+    "acc_batch_launch": ([_P, _P], _I),
+    "acc_batch_status": ([_P, _P], _I),
+    "acc_batch_destroy": ([_P], _I),
+    "acc_batch_autotune": ([ctypes.c_char_p, _P], _I),
+    "acc_batch_load_tuning": ([ctypes.c_char_p], _I),
 }
 
 
@@ -335,3 +342,74 @@ def stencil2(wa, wb, a: torch.Tensor, b: torch.Tensor, boundary_a="clamp", bound
                                   _ptr(out), _stream(stream))
     _check(st, "stencil2")
     return out
+
+
+# ----------------------------------------------------------------- batches
+REQ_FOLD, REQ_SCAN = 0, 1
+
+
+class Request(ctypes.Structure):
+    """struct acc_request of acc_gb300.h."""
+    _fields_ = [("kind", ctypes.c_int), ("type", ctypes.c_int), ("inp", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("n", ctypes.c_int64), ("has_seed", ctypes.c_int), ("seed", ctypes.c_uint64)]
+
+
+def _seed_bits(type_code: int, value) -> int:
+    c = _CTYPES[type_code](value)
+    return int.from_bytes(bytes(c), "little")
+
+
+class Batch:
+    """Many fold / scanl1 requests in one persistent launch (acc_batch_*).
+
+    `requests` is a list of (kind, xs, out, seed): kind "fold" (out: one
+    element) or "scan" (out: len(xs) elements), seed None for fold1 /
+    seedless scanl1.  Every request uses the primitive `f` ('+', 'min' or 'max')."""
+
+    def __init__(self, f, requests):
+        self._keep = []
+        arr = (Request * max(1, len(requests)))()
+        for i, (kind, xs, out, seed) in enumerate(requests):
+            xs = _dev(xs)
+            tc = type_of(xs)
+            self._keep += [xs, out]
+            arr[i].kind = REQ_FOLD if kind == "fold" else REQ_SCAN
+            arr[i].type = tc
+            arr[i].inp = xs.data_ptr()
+            arr[i].out = out.data_ptr()
+            arr[i].n = xs.numel()
+            arr[i].has_seed = 0 if seed is None else 1
+            arr[i].seed = 0 if seed is None else _seed_bits(tc, seed)
+        self._reqs = arr
+        self._h = ctypes.c_void_p()
+        _check(lib().acc_batch_create(op_of(f), ctypes.cast(arr, ctypes.c_void_p), len(requests),
+                                      ctypes.byref(self._h)), "acc_batch_create")
+
+    def capture(self, stream=None):
+        _check(lib().acc_batch_capture(self._h, _stream(stream)), "acc_batch_capture")
+
+    def launch(self, stream=None):
+        _check(lib().acc_batch_launch(self._h, _stream(stream)), "acc_batch_launch")
+
+    def status(self, stream=None):
+        _check(lib().acc_batch_status(self._h, _stream(stream)), "acc_batch_status")
+
+    def close(self):
+        if self._h:
+            lib().acc_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_autotune(table_path=None, stream=None):
+    """Run the batch tile-size autotuner (acc_batch_autotune)."""
+    _check(lib().acc_batch_autotune(table_path.encode() if table_path else None, _stream(stream)), "autotune")
+
+
+def batch_load_tuning(table_path):
+    _check(lib().acc_batch_load_tuning(str(table_path).encode()), "load tuning")

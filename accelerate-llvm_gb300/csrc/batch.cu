@@ -1,0 +1,595 @@
+// batch.cu -- many independent fold / scanl1 requests in ONE persistent launch,
+// replayable as a CUDA graph, with tile sizes from the library's autotuner.
+//
+// The reference launches every skeleton separately, each with host-side
+// set-up (PTX/Execute.hs:835-881); thousands of small and medium requests are
+// dominated by launch latency.  Here a plan flattens a batch into work items
+// (request, tile), each request cut into tiles of 256 x IPT elements, IPT
+// chosen per (kind, type, size bucket) by the autotuner.  One persistent
+// kernel draws items from an atomic ticket in table order:
+//   * fold tiles reduce their chunk (16-byte vector loads); the last tile of
+//     a request (per-request atomic ticket) folds the tile partials in order
+//     and writes z `f` result;
+//   * scan tiles stage their chunk in shared memory, scan it, and take the
+//     prefix of the earlier tiles of the same request by decoupled look-back
+//     (items are drawn in order, so every predecessor tile belongs to a
+//     running CTA).
+// All scratch is owned by the plan and allocated when the plan is made; a
+// launch allocates nothing and takes its look-back epoch from a device word
+// that the last CTA advances, so a captured graph replays unchanged.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+
+namespace accgb {
+
+constexpr int BT = 256;                    // threads per CTA
+constexpr int B_MAX_TILE_BYTES = 32768;    // largest tile staged in shared memory
+
+struct BReq {
+  const void *in;
+  void *out;
+  int64_t n;
+  uint64_t seed;
+  int64_t first_item;
+  int64_t ntiles;
+  int32_t kind, type, has_seed, ipt;
+};
+
+struct BatchArgs {
+  const BReq *reqs;
+  const int32_t *item_req;
+  int64_t nitems;
+  uint64_t *status;      // 2 words per item (scan look-back)
+  uint64_t *partials;    // one state per item (fold)
+  uint32_t *req_ticket;  // per request, zero between launches
+  uint32_t *words;       // [0] error, [1] item ticket, [2] epoch
+};
+
+// ---------------------------------------------------------------- device parts
+template <class S>
+__device__ __forceinline__ void b_publish(uint64_t *status, int64_t t, uint32_t epoch, uint32_t flag, S v) {
+  uint64_t b = to_bits(v);
+  uint64_t tag = (uint64_t)((epoch << 2) | flag) << 32;
+  if constexpr (sizeof(S) == 8) st_relaxed_u64(status + 2 * t + 1, tag | (b >> 32));
+  st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
+}
+template <class S>
+__device__ __forceinline__ uint32_t b_peek(const uint64_t *status, int64_t t, uint32_t epoch, S &v) {
+  uint64_t w0 = ld_relaxed_u64(status + 2 * t);
+  uint32_t tag = (uint32_t)(w0 >> 32);
+  if ((tag >> 2) != epoch) return 0;
+  uint64_t b = w0 & 0xffffffffull;
+  if constexpr (sizeof(S) == 8) {
+    uint64_t w1 = ld_relaxed_u64(status + 2 * t + 1);
+    if ((uint32_t)(w1 >> 32) != tag) return 0;
+    b |= (w1 & 0xffffffffull) << 32;
+  }
+  v = from_bits<S>(b);
+  return tag & 3u;
+}
+
+// CTA-wide ordered reduction (valid in thread 0).
+template <class A>
+__device__ __forceinline__ typename A::S b_block_reduce(typename A::S v, typename A::S *s_part) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_reduce<A>(v);
+  if (lane == 0) s_part[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < BT / 32 ? s_part[lane] : A::id();
+    v = warp_reduce<A>(v);
+  }
+  __syncthreads();
+  return v;
+}
+
+template <int OP, class T, int PREC>
+__device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int32_t r, unsigned char *smem) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  __shared__ bool s_last;
+  S *s_part = reinterpret_cast<S *>(smem);
+  const int64_t tile = item - q.first_item;
+  const int64_t ts = (int64_t)q.ipt * BT;
+  const int64_t b = tile * ts;
+  const int64_t e = b + ts < q.n ? b + ts : q.n;
+  const T *src = static_cast<const T *>(q.in) + b;
+  const int64_t len = e - b;
+  // 16-byte vector body, scalar head and tail.
+  constexpr int VEC = 16 / sizeof(T);
+  S acc = A::id();
+  const uintptr_t addr = reinterpret_cast<uintptr_t>(src);
+  int64_t head = (int64_t)(((16u - (addr & 15u)) & 15u) / sizeof(T));
+  if (head > len) head = len;
+  if ((int64_t)threadIdx.x < head) acc = A::push(acc, src[threadIdx.x]);
+  const int64_t nvec = (len - head) / VEC;
+  const uint4 *qv = reinterpret_cast<const uint4 *>(src + head);
+  for (int64_t i = threadIdx.x; i < nvec; i += BT) {
+    uint4 v = ld_stream16(qv + i);
+    T el[VEC];
+    memcpy(el, &v, 16);
+#pragma unroll
+    for (int k = 0; k < VEC; ++k) acc = A::push(acc, el[k]);
+  }
+  const int64_t tail0 = head + nvec * VEC;
+  if (tail0 + threadIdx.x < len) acc = A::push(acc, src[tail0 + threadIdx.x]);
+  acc = b_block_reduce<A>(acc, s_part);
+  S *parts = reinterpret_cast<S *>(a.partials);
+  if (threadIdx.x == 0) {
+    parts[item] = acc;
+    __threadfence();
+    const uint32_t prev = atomicAdd(a.req_ticket + r, 1u);
+    s_last = prev == (uint32_t)(q.ntiles - 1);
+  }
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    S v = A::id();
+    const int64_t per = (q.ntiles + BT - 1) / BT;
+    const int64_t lo = threadIdx.x * per, hi = lo + per < q.ntiles ? lo + per : q.ntiles;
+    for (int64_t i = lo; i < hi; ++i) v = A::comb(v, ld_state<S>(&parts[q.first_item + i]));
+    v = b_block_reduce<A>(v, s_part);
+    if (threadIdx.x == 0) {
+      if (q.has_seed) v = A::comb(A::lift(from_bits<T>(q.seed)), v);
+      *static_cast<T *>(q.out) = A::lower(v);
+      a.req_ticket[r] = 0u;  // re-arm for the next launch
+    }
+  }
+  __syncthreads();
+}
+
+template <int OP, class T, int PREC>
+__device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uint32_t epoch, unsigned char *smem) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  __shared__ S s_warp[BT / 32];
+  __shared__ S s_prefix;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ipt = q.ipt;
+  const int pitch = ipt + 1;  // padded row: conflict-free thread-per-row access
+  T *tile_s = reinterpret_cast<T *>(smem + 256);
+  const int64_t tile = item - q.first_item;
+  const int64_t ts = (int64_t)ipt * BT;
+  const int64_t b = tile * ts;
+  const T idT = Prim<OP, T>::id();
+  const T *src = static_cast<const T *>(q.in);
+  for (int k = tid; k < ts; k += BT) {
+    const int64_t gi = b + k;
+    tile_s[(k / ipt) * pitch + (k % ipt)] = gi < q.n ? src[gi] : idT;
+  }
+  __syncthreads();
+  T *row = tile_s + tid * pitch;
+  S agg = A::lift(row[0]);
+  for (int j = 1; j < ipt; ++j) agg = A::push(agg, row[j]);
+  S incl = warp_scan_incl<A>(agg);
+  S up = shfl_up(incl, 1);
+  const S excl_lane = lane == 0 ? A::id() : up;
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  S wpre = A::id();
+  for (int w = 0; w < warp; ++w) wpre = A::comb(wpre, s_warp[w]);
+  if (warp == 0) {
+    S bagg = s_warp[0];
+    for (int w = 1; w < BT / 32; ++w) bagg = A::comb(bagg, s_warp[w]);
+    S prefix = q.has_seed ? A::lift(from_bits<T>(q.seed)) : A::id();
+    if (tile > 0) {
+      if (lane == 0) b_publish<S>(a.status, item, epoch, 1u, bagg);
+      S acc = A::id();
+      int64_t k0 = 0;
+      bool gave_up = false;
+      while (true) {
+        const int64_t d = k0 + lane;
+        const bool exists = d < tile;  // predecessors of the same request only
+        const int64_t pt = item - 1 - d;
+        uint32_t flag = exists ? 0u : 2u;
+        S v = A::id();
+        uint32_t it = 0;
+        while (true) {
+          if (exists && flag == 0) flag = b_peek<S>(a.status, pt, epoch, v);
+          if (__all_sync(0xffffffffu, flag != 0)) break;
+          ++it;
+          const bool stop = gave_up || it > SPIN_LIMIT ||
+                            ((it & 63u) == 0 && (ld_relaxed_u32(a.words) & DEV_ERR_TIMEOUT) != 0u);
+          if (__any_sync(0xffffffffu, stop)) {
+            gave_up = true;
+            if (lane == 0) raise_error(a.words, DEV_ERR_TIMEOUT);
+            if (flag == 0) flag = 2u;
+            break;
+          }
+          __nanosleep(it < 8 ? 32 : 128);
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, flag == 2u);
+        const int kp = pm ? __ffs(pm) - 1 : 32;
+        if (lane > kp) v = A::id();
+        S wv = warp_reduce_rev<A>(v);
+        wv = shfl_idx(wv, 0);
+        acc = A::comb(wv, acc);
+        if (pm) break;
+        k0 += 32;
+      }
+      prefix = acc;  // the seed already sits in the request's first tile
+    }
+    if (lane == 0) {
+      b_publish<S>(a.status, item, epoch, 2u, A::comb(prefix, bagg));
+      s_prefix = prefix;
+    }
+  }
+  __syncthreads();
+  S run = A::comb(s_prefix, A::comb(wpre, excl_lane));
+  for (int j = 0; j < ipt; ++j) {
+    run = A::push(run, row[j]);
+    row[j] = A::lower(run);
+  }
+  __syncthreads();
+  T *dst = static_cast<T *>(q.out);
+  for (int k = tid; k < ts; k += BT) {
+    const int64_t gi = b + k;
+    if (gi < q.n) dst[gi] = tile_s[(k / ipt) * pitch + (k % ipt)];
+  }
+  __syncthreads();
+}
+
+enum { BK_FOLD = 0, BK_SCAN = 1 };
+
+template <int OP>
+__global__ void __launch_bounds__(BT) batch_kernel(BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int64_t s_item;
+  __shared__ BReq s_req;
+  __shared__ uint32_t s_epoch;
+  if (threadIdx.x == 0) s_epoch = (ld_relaxed_u32(a.words + 2) & ((1u << 29) - 1)) + 1;
+  const uint32_t last_ticket = (uint32_t)a.nitems + gridDim.x - 1;
+  while (true) {
+    if (threadIdx.x == 0) {
+      const uint32_t t = atomicAdd(a.words + 1, 1u);
+      if (t == last_ticket) {
+        // Every CTA has drawn its last ticket (and read the epoch): re-arm the
+        // ticket and advance the epoch for the next launch or graph replay.
+        a.words[1] = 0u;
+        atomicAdd(a.words + 2, 1u);
+      }
+      s_item = (int64_t)t < a.nitems ? (int64_t)t : -1;
+      if (s_item >= 0) s_req = a.reqs[a.item_req[s_item]];
+    }
+    __syncthreads();
+    const int64_t item = s_item;
+    if (item < 0) break;
+    const BReq q = s_req;
+    const int32_t r = a.item_req[item];
+    const uint32_t epoch = s_epoch;
+    if (q.kind == BK_FOLD) {
+      switch (q.type) {
+        case ACC_I32: b_fold_tile<OP, int32_t, 0>(a, q, item, r, smem); break;
+        case ACC_I64: b_fold_tile<OP, int64_t, 0>(a, q, item, r, smem); break;
+        case ACC_F32: b_fold_tile<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN>(a, q, item, r, smem); break;
+        default: b_fold_tile<OP, double, 0>(a, q, item, r, smem); break;
+      }
+    } else {
+      switch (q.type) {
+        case ACC_I32: b_scan_tile<OP, int32_t, 0>(a, q, item, epoch, smem); break;
+        case ACC_I64: b_scan_tile<OP, int64_t, 0>(a, q, item, epoch, smem); break;
+        case ACC_F32: b_scan_tile<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN>(a, q, item, epoch, smem); break;
+        default: b_scan_tile<OP, double, 0>(a, q, item, epoch, smem); break;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- autotuner table
+// Elements per thread (IPT) per (kind, type, log2 size bucket); the tile is
+// 256 x IPT elements.  Filled by acc_batch_autotune, persisted as JSON.
+struct TuneKey {
+  int kind, type, bucket;
+  bool operator<(const TuneKey &o) const { return std::tie(kind, type, bucket) < std::tie(o.kind, o.type, o.bucket); }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, int> g_tune;
+
+static int type_bytes(int type) { return (type == ACC_I64 || type == ACC_F64) ? 8 : 4; }
+static int max_ipt(int type) { return B_MAX_TILE_BYTES / (BT * type_bytes(type)); }
+static int bucket_of(int64_t n) {
+  int b = 0;
+  while (b < 62 && (int64_t(1) << (b + 1)) <= n) ++b;
+  return b;
+}
+static int default_ipt(int kind, int type, int64_t n) {
+  // Before tuning: one wave of small tiles for small requests, large tiles otherwise.
+  const int cap = max_ipt(type);
+  int ipt = n <= (1 << 14) ? 4 : n <= (1 << 18) ? 8 : 16;
+  (void)kind;
+  return ipt < cap ? ipt : cap;
+}
+static int tuned_ipt(int kind, int type, int64_t n) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(TuneKey{kind, type, bucket_of(n)});
+  if (it != g_tune.end()) return it->second;
+  return default_ipt(kind, type, n);
+}
+
+// ---------------------------------------------------------------- plan
+struct Batch {
+  int op;
+  int device;
+  int64_t count = 0, nitems = 0;
+  BReq *d_reqs = nullptr;
+  int32_t *d_item_req = nullptr;
+  uint64_t *d_status = nullptr;
+  uint64_t *d_partials = nullptr;
+  uint32_t *d_req_ticket = nullptr;
+  uint32_t *d_words = nullptr;
+  int grid = 0;
+  size_t smem = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+template <int OP> static void *batch_kernel_ptr() { return reinterpret_cast<void *>(batch_kernel<OP>); }
+
+static int batch_launch_raw(Batch *b, cudaStream_t s) {
+  BatchArgs a{b->d_reqs, b->d_item_req, b->nitems, b->d_status, b->d_partials, b->d_req_ticket, b->d_words};
+  switch (b->op) {
+    case ACC_ADD: batch_kernel<ACC_ADD><<<b->grid, BT, b->smem, s>>>(a); break;
+    case ACC_MIN: batch_kernel<ACC_MIN><<<b->grid, BT, b->smem, s>>>(a); break;
+    default: batch_kernel<ACC_MAX><<<b->grid, BT, b->smem, s>>>(a); break;
+  }
+  return check_launch();
+}
+
+static void batch_free(Batch *b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  cudaFree(b->d_reqs);
+  cudaFree(b->d_item_req);
+  cudaFree(b->d_status);
+  cudaFree(b->d_partials);
+  cudaFree(b->d_req_ticket);
+  cudaFree(b->d_words);
+  delete b;
+}
+
+static int batch_make(int op, const acc_request *reqs, int64_t count, const int32_t *ipt_override, Batch **out) {
+  if (op != ACC_ADD && op != ACC_MIN && op != ACC_MAX) return ACC_ERR_UNSUPPORTED;
+  if (count < 0 || (count > 0 && !reqs) || count > (1ll << 31) - 1) return ACC_ERR_INVALID;
+  std::vector<BReq> h(count);
+  std::vector<int32_t> item_req;
+  int64_t nitems = 0;
+  size_t max_tile = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const acc_request &q = reqs[i];
+    if (q.kind != ACC_REQ_FOLD && q.kind != ACC_REQ_SCAN) return ACC_ERR_INVALID;
+    if (q.type != ACC_I32 && q.type != ACC_I64 && q.type != ACC_F32 && q.type != ACC_F64) return ACC_ERR_UNSUPPORTED;
+    if (q.n < 0 || (q.n > 0 && (!q.in || !q.out))) return ACC_ERR_INVALID;
+    if (q.kind == ACC_REQ_FOLD && q.n == 0 && !q.has_seed) return ACC_ERR_EMPTY;
+    int ipt = ipt_override ? ipt_override[i] : tuned_ipt(q.kind, q.type, q.n);
+    if (ipt < 1) ipt = 1;
+    if (ipt > max_ipt(q.type)) ipt = max_ipt(q.type);
+    const int64_t ts = (int64_t)ipt * BT;
+    int64_t nt = (q.n + ts - 1) / ts;
+    if (q.kind == ACC_REQ_FOLD && nt == 0) nt = 1;  // fold z [] = z: one (empty) tile writes the seed
+    BReq &r = h[i];
+    r.in = q.in; r.out = q.out; r.n = q.n; r.seed = q.seed;
+    r.kind = q.kind; r.type = q.type; r.has_seed = q.has_seed; r.ipt = ipt;
+    r.first_item = nitems; r.ntiles = nt;
+    for (int64_t k = 0; k < nt; ++k) item_req.push_back((int32_t)i);
+    nitems += nt;
+    const size_t tb = (size_t)(ipt + 1) * BT * type_bytes(q.type) + 256;
+    if (tb > max_tile) max_tile = tb;
+  }
+  if (nitems >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
+  Batch *b = new Batch();
+  b->op = op;
+  cudaGetDevice(&b->device);
+  b->count = count;
+  b->nitems = nitems;
+  b->smem = max_tile < 1024 ? 1024 : max_tile;
+  auto fail = [&](cudaError_t e) { batch_free(b); return cuda_status(e); };
+  cudaError_t e;
+  if ((e = cudaMalloc(&b->d_reqs, sizeof(BReq) * (count ? count : 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&b->d_item_req, sizeof(int32_t) * (nitems ? nitems : 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&b->d_status, sizeof(uint64_t) * 2 * (nitems ? nitems : 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&b->d_partials, sizeof(uint64_t) * (nitems ? nitems : 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&b->d_req_ticket, sizeof(uint32_t) * (count ? count : 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&b->d_words, sizeof(uint32_t) * 64)) != cudaSuccess) return fail(e);
+  if (count) cudaMemcpy(b->d_reqs, h.data(), sizeof(BReq) * count, cudaMemcpyHostToDevice);
+  if (nitems) cudaMemcpy(b->d_item_req, item_req.data(), sizeof(int32_t) * nitems, cudaMemcpyHostToDevice);
+  cudaMemset(b->d_status, 0, sizeof(uint64_t) * 2 * (nitems ? nitems : 1));
+  cudaMemset(b->d_req_ticket, 0, sizeof(uint32_t) * (count ? count : 1));
+  cudaMemset(b->d_words, 0, sizeof(uint32_t) * 64);
+  void *kern = op == ACC_ADD ? batch_kernel_ptr<ACC_ADD>() : op == ACC_MIN ? batch_kernel_ptr<ACC_MIN>()
+                                                                          : batch_kernel_ptr<ACC_MAX>();
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, b->smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  int64_t grid = (int64_t)device_info().sms * per_sm;
+  if (grid > nitems) grid = nitems > 0 ? nitems : 1;
+  b->grid = (int)grid;
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+  *out = b;
+  return ACC_OK;
+}
+
+// ---------------------------------------------------------------- autotune
+static int autotune_run(int kind, int type, int bucket, cudaStream_t s, void *buf, size_t buf_bytes, int *best) {
+  const int64_t n = int64_t(1) << bucket;
+  const int eb = type_bytes(type);
+  // A batch of equal requests of this bucket's size, up to 2^24 elements in all.
+  int64_t count = std::max<int64_t>(1, std::min<int64_t>(4096, (int64_t(1) << 24) / n));
+  while (count > 1 && (size_t)(count * n * eb * 2 + count * 8) > buf_bytes) count /= 2;
+  std::vector<acc_request> reqs(count);
+  char *base = static_cast<char *>(buf);
+  for (int64_t i = 0; i < count; ++i) {
+    acc_request &q = reqs[i];
+    q.kind = kind; q.type = type; q.n = n; q.has_seed = 0; q.seed = 0;
+    q.in = base;                                  // all requests read the same input
+    q.out = base + (size_t)n * eb + (kind == ACC_REQ_SCAN ? (size_t)i * n * eb : (size_t)i * eb);
+  }
+  float best_ms = 1e30f;
+  int best_ipt = default_ipt(kind, type, n);
+  for (int ipt = 1; ipt <= max_ipt(type); ipt *= 2) {
+    std::vector<int32_t> ov(count, ipt);
+    Batch *b = nullptr;
+    int st = batch_make(ACC_ADD, reqs.data(), count, ov.data(), &b);
+    if (st) return st;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    batch_launch_raw(b, s);
+    cudaEventRecord(e0, s);
+    for (int rep = 0; rep < 3; ++rep) batch_launch_raw(b, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    batch_free(b);
+    if (ms < best_ms) { best_ms = ms; best_ipt = ipt; }
+  }
+  *best = best_ipt;
+  return check_launch();
+}
+
+}  // namespace accgb
+
+using namespace accgb;
+
+extern "C" int acc_batch_create(int op, const acc_request *reqs, int64_t count, acc_batch **out) {
+  if (!out) return ACC_ERR_INVALID;
+  Batch *b = nullptr;
+  int st = batch_make(op, reqs, count, nullptr, &b);
+  if (st) return st;
+  *out = reinterpret_cast<acc_batch *>(b);
+  return ACC_OK;
+}
+
+extern "C" int acc_batch_launch(acc_batch *batch, void *stream) {
+  Batch *b = reinterpret_cast<Batch *>(batch);
+  if (!b) return ACC_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (b->nitems == 0) return ACC_OK;
+  if (b->exec) return cuda_status(cudaGraphLaunch(b->exec, s));
+  return batch_launch_raw(b, s);
+}
+
+extern "C" int acc_batch_capture(acc_batch *batch, void *stream) {
+  Batch *b = reinterpret_cast<Batch *>(batch);
+  if (!b) return ACC_ERR_INVALID;
+  if (b->exec || b->nitems == 0) return ACC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaStream_t cap = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    batch_launch_raw(b, cap);
+    e = cudaStreamEndCapture(cap, &b->graph);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  cudaStreamDestroy(cap);
+  (void)s;
+  return cuda_status(e);
+}
+
+extern "C" int acc_batch_status(acc_batch *batch, void *stream) {
+  Batch *b = reinterpret_cast<Batch *>(batch);
+  if (!b) return ACC_ERR_INVALID;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e);
+  uint32_t err = 0;
+  e = cudaMemcpy(&err, b->d_words, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (!err) return ACC_OK;
+  cudaMemset(b->d_words, 0, sizeof(uint32_t) * 64);
+  cudaMemset(b->d_status, 0, sizeof(uint64_t) * 2 * (b->nitems ? b->nitems : 1));
+  cudaMemset(b->d_req_ticket, 0, sizeof(uint32_t) * (b->count ? b->count : 1));
+  return ACC_ERR_TIMEOUT;
+}
+
+extern "C" int acc_batch_destroy(acc_batch *batch) {
+  Batch *b = reinterpret_cast<Batch *>(batch);
+  if (b) {
+    cudaDeviceSynchronize();
+    batch_free(b);
+  }
+  return ACC_OK;
+}
+
+extern "C" int acc_batch_autotune(const char *table_path, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t buf_bytes = (size_t)1 << 28;
+  void *buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, buf_bytes);
+  if (e != cudaSuccess) return cuda_status(e);
+  cudaMemset(buf, 0, buf_bytes);
+  std::map<TuneKey, int> table;
+  const int kinds[2] = {ACC_REQ_FOLD, ACC_REQ_SCAN};
+  const int types[4] = {ACC_I32, ACC_F32, ACC_I64, ACC_F64};
+  int st = ACC_OK;
+  for (int kind : kinds)
+    for (int type : types)
+      for (int bucket = 8; bucket <= 22 && st == ACC_OK; ++bucket) {
+        int best = 0;
+        st = autotune_run(kind, type, bucket, s, buf, buf_bytes, &best);
+        if (st == ACC_OK) table[TuneKey{kind, type, bucket}] = best;
+      }
+  cudaFree(buf);
+  if (st) return st;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (auto &kv : table) g_tune[kv.first] = kv.second;
+  }
+  if (table_path) {
+    FILE *f = fopen(table_path, "w");
+    if (!f) return ACC_ERR_INVALID;
+    cudaDeviceProp p;
+    cudaGetDeviceProperties(&p, 0);
+    fprintf(f, "{\"gpu\": \"%s\", \"threads\": %d, \"entries\": [", p.name, BT);
+    bool first = true;
+    for (auto &kv : table) {
+      fprintf(f, "%s[%d, %d, %d, %d]", first ? "" : ", ", kv.first.kind, kv.first.type, kv.first.bucket, kv.second);
+      first = false;
+    }
+    fprintf(f, "]}\n");
+    fclose(f);
+  }
+  return ACC_OK;
+}
+
+extern "C" int acc_batch_load_tuning(const char *table_path) {
+  if (!table_path) return ACC_ERR_INVALID;
+  FILE *f = fopen(table_path, "r");
+  if (!f) return ACC_ERR_INVALID;
+  std::string text;
+  char chunk[4096];
+  size_t got;
+  while ((got = fread(chunk, 1, sizeof(chunk), f)) > 0) text.append(chunk, got);
+  fclose(f);
+  const size_t at = text.find("\"entries\"");
+  if (at == std::string::npos) return ACC_ERR_INVALID;
+  std::map<TuneKey, int> table;
+  const char *p = text.c_str() + at;
+  while ((p = strchr(p, '[')) != nullptr) {
+    int kind, type, bucket, ipt;
+    if (sscanf(p, "[%d, %d, %d, %d]", &kind, &type, &bucket, &ipt) == 4) table[TuneKey{kind, type, bucket}] = ipt;
+    ++p;
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  for (auto &kv : table) g_tune[kv.first] = kv.second;
+  return ACC_OK;
+}

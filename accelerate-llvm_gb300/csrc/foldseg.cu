@@ -18,6 +18,9 @@
 // segment gives z with a seed and is left unwritten without one
 // (PTX/CodeGen/FoldSeg.hs:170-178).  Offsets that decrease or run past the
 // row are skipped and raise ACC_ERR_INDEX instead of reading out of bounds.
+#include <cstdlib>
+#include <cstring>
+
 #include "common.cuh"
 
 namespace accgb {
@@ -172,6 +175,384 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
   }
 }
 
+// ----------------------------------------------------------------- segmented single pass
+// Rows of 1-D values with 16-byte aligned storage take this path: the values
+// are cut into tiles of 256 rows x 128 B (TMA, 128-byte swizzle, as in the
+// scan), independent of the segment lengths, so every CTA streams the same
+// number of bytes however skewed the segmentation is.
+//   pre-pass  seg_tiles_kernel: tile_seg[k] = the segment that contains the
+//             first element of tile k; empty segments get their seed here.
+//   main      foldseg_scan_kernel: a tile's segment ENDS (off[s+1], tile-
+//             relative, 16-bit) go to shared memory; each thread folds its
+//             128-byte row, restarting after every end; rows combine with a
+//             segmented warp / CTA scan ((f1,v1).(f2,v2) = (f1|f2, f2 ? v2 :
+//             v1 `f` v2)); the value carried into the tile comes from a
+//             segmented decoupled look-back that stops at the first
+//             predecessor holding an end; a second pass over the row writes
+//             z `f` (segment) where each segment's last element lies.
+constexpr int FS_THREADS = 256;
+constexpr int FS_ROW_BYTES = 128;
+constexpr int FS_CAP = 2048;  // segment ends per tile held in shared memory
+
+struct SegScanArgs {
+  const void *in;
+  const void *off;
+  void *out;
+  int64_t inner, nseg;
+  int off64;
+  uint64_t seed;
+  int has_seed;
+  int64_t full_rows, ntiles;
+  int64_t *tile_seg;
+  uint64_t *status;
+  uint32_t *ticket;
+  uint32_t *err;
+  uint32_t epoch;
+};
+
+__device__ __forceinline__ int64_t seg_off2(const SegScanArgs &a, int64_t i) {
+  return a.off64 ? static_cast<const int64_t *>(a.off)[i] : (int64_t) static_cast<const int32_t *>(a.off)[i];
+}
+
+template <class T>
+__global__ void seg_tiles_kernel(SegScanArgs a, int64_t tile_elems) {
+  const T z = from_bits<T>(a.seed);
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.nseg; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = seg_off2(a, s), v = seg_off2(a, s + 1);
+    if (u < 0 || v < u || v > a.inner) { raise_error(a.err, DEV_ERR_INDEX); continue; }
+    if (u == v) {
+      if (a.has_seed) static_cast<T *>(a.out)[s] = z;
+      continue;
+    }
+    for (int64_t k = (u + tile_elems - 1) / tile_elems; k * tile_elems < v; ++k) a.tile_seg[k] = s;
+  }
+}
+
+// Look-back slot of the segmented scan: tag = epoch << 3 | end-seen << 2 | flag.
+template <class S>
+__device__ __forceinline__ void publish_seg(uint64_t *status, int64_t t, uint32_t epoch, uint32_t flag, bool end, S v) {
+  uint64_t b = to_bits(v);
+  uint64_t tag = (uint64_t)((epoch << 3) | ((uint32_t)end << 2) | flag) << 32;
+  if constexpr (sizeof(S) == 8) st_relaxed_u64(status + 2 * t + 1, tag | (b >> 32));
+  st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
+}
+template <class S>
+__device__ __forceinline__ uint32_t peek_seg(const uint64_t *status, int64_t t, uint32_t epoch, S &v, bool &end) {
+  uint64_t w0 = ld_relaxed_u64(status + 2 * t);
+  uint32_t tag = (uint32_t)(w0 >> 32);
+  if ((tag >> 3) != epoch) return 0;
+  uint64_t b = w0 & 0xffffffffull;
+  if constexpr (sizeof(S) == 8) {
+    uint64_t w1 = ld_relaxed_u64(status + 2 * t + 1);
+    if ((uint32_t)(w1 >> 32) != tag) return 0;
+    b |= (w1 & 0xffffffffull) << 32;
+  }
+  v = from_bits<S>(b);
+  end = (tag >> 2) & 1u;
+  return tag & 3u;
+}
+
+template <int OP, class T, int PREC>
+__global__ void __launch_bounds__(FS_THREADS, 3)
+foldseg_scan_kernel(const __grid_constant__ CUtensorMap tin, SegScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  constexpr int ITEMS = FS_ROW_BYTES / sizeof(T);
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int TE = FS_THREADS * ITEMS;
+  constexpr int NWARP = FS_THREADS / 32;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t bar;
+  __shared__ int64_t s_tile, s_lo, s_cnt, s_off0;
+  __shared__ uint16_t s_end[FS_CAP];
+  __shared__ S s_warp[NWARP];
+  __shared__ int s_wend[NWARP];
+  __shared__ S s_carry;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T idT = Prim<OP, T>::id();
+
+  if (tid == 0) {
+    const uint32_t dyn = atomicAdd(a.ticket, 1u);
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    const int64_t tile = dyn;
+    s_tile = tile;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_expect_tx(&bar, FS_THREADS * FS_ROW_BYTES);
+    tma_load_2d(buf, &tin, 0, (int)(tile * FS_THREADS), &bar);
+    const int64_t b = tile * TE;
+    const int64_t off0 = seg_off2(a, 0);
+    auto first_seg = [&](int64_t k) -> int64_t {
+      if (k >= a.ntiles) return a.nseg;
+      const int64_t s = a.tile_seg[k];
+      if (s >= 0) return s;
+      return k * TE < off0 ? 0 : a.nseg;  // tile starts before the first / after the last segment
+    };
+    const int64_t lo = first_seg(tile), hi = first_seg(tile + 1);
+    s_lo = lo;
+    s_cnt = hi > lo ? hi - lo : 0;
+    s_off0 = off0 > b ? off0 - b : 0;  // elements of this tile before the first segment
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t b = tile * TE;
+  const int64_t lo = s_lo, cnt = s_cnt;
+  const int off0 = (int)(s_off0 < TE ? s_off0 : TE);
+  const bool in_smem_list = cnt <= FS_CAP;
+  // Segment s_lo + i ends at tile-relative position end(i) (exclusive).
+  if (in_smem_list) {
+    for (int64_t i = tid; i < cnt; i += FS_THREADS) {
+      int64_t e = seg_off2(a, lo + 1 + i) - b;
+      if (e < 1 || e > TE) { raise_error(a.err, DEV_ERR_INDEX); e = TE + 1; }
+      s_end[i] = (uint16_t)(e > TE ? 0xffff : e);
+    }
+  }
+  __syncthreads();
+  auto end_at = [&](int64_t i) -> int {
+    if (i >= cnt) return 1 << 30;
+    if (in_smem_list) return s_end[i];
+    const int64_t e = seg_off2(a, lo + 1 + i) - b;
+    return (e < 1 || e > TE) ? 1 << 30 : (int)e;
+  };
+  if (!mbar_wait(&bar, 0)) {
+    raise_error(a.err, DEV_ERR_TIMEOUT);
+    mbar_wait(&bar, 0);
+  }
+
+  const int r0 = tid * ITEMS;
+  const int64_t grow = tile * FS_THREADS + tid;
+  auto load_row = [&](T (&x)[ITEMS]) {
+    if (grow < a.full_rows) {
+#pragma unroll
+      for (int c = 0; c < ITEMS / VEC; ++c) {
+        uint4 v = *reinterpret_cast<const uint4 *>(buf + tid * FS_ROW_BYTES + ((c ^ (tid & 7)) << 4));
+        memcpy(&x[c * VEC], &v, 16);
+      }
+    } else {
+      const T *src = static_cast<const T *>(a.in);
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) x[j] = (b + r0 + j < a.inner) ? src[b + r0 + j] : idT;
+    }
+    if (r0 < off0) {
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j)
+        if (r0 + j < off0) x[j] = idT;  // not part of any segment
+    }
+  };
+  // First end strictly after this row's start: binary search.
+  int64_t i0;
+  {
+    int64_t l = 0, h = cnt;
+    while (l < h) {
+      const int64_t m = (l + h) >> 1;
+      if (end_at(m) <= r0) l = m + 1; else h = m;
+    }
+    i0 = l;
+  }
+
+  // Ends inside this row as a bit mask: bit j set when a segment ends right
+  // after element j (several list entries at one position are the empty
+  // segments that follow a non-empty one).
+  uint32_t emask = 0;
+  {
+    int64_t i = i0;
+    int e = end_at(i);
+    while (e <= r0 + ITEMS) {
+      emask |= 1u << (e - r0 - 1);
+      e = end_at(++i);
+    }
+  }
+
+  // ---- pass 1: row value since its last end (branch-free), and whether it holds an end
+  S acc = A::id();
+  const bool ended = emask != 0u;
+  {
+    T x[ITEMS];
+    load_row(x);
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      acc = A::push(acc, x[j]);
+      if ((emask >> j) & 1u) acc = A::id();
+    }
+  }
+  // Segmented inclusive warp scan: (f1, v1) . (f2, v2) = (f1 | f2, f2 ? v2 : v1 `f` v2).
+  S incl = acc;
+  bool fin = ended;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const S ov = shfl_up(incl, d);
+    const bool of = __shfl_up_sync(0xffffffffu, fin, d);
+    if (lane >= d) {
+      if (!fin) incl = A::comb(ov, incl);
+      fin = fin || of;
+    }
+  }
+  S ex = shfl_up(incl, 1);
+  bool exf = __shfl_up_sync(0xffffffffu, fin, 1);
+  if (lane == 0) { ex = A::id(); exf = false; }
+  if (lane == 31) { s_warp[warp] = incl; s_wend[warp] = fin; }
+  __syncthreads();
+  S wv = A::id();
+  bool wf = false;
+  for (int w = 0; w < warp; ++w) {
+    wv = s_wend[w] ? s_warp[w] : A::comb(wv, s_warp[w]);
+    wf = wf || s_wend[w];
+  }
+
+  // ---- segmented look-back (warp 0): the value of the segment open at the tile start
+  if (warp == 0) {
+    S tv = A::id();
+    bool tf = false;
+    for (int w = 0; w < NWARP; ++w) {
+      tv = s_wend[w] ? s_warp[w] : A::comb(tv, s_warp[w]);
+      tf = tf || s_wend[w];
+    }
+    S carry = A::id();
+    if (tile > 0) {
+      if (lane == 0) publish_seg<S>(a.status, tile, a.epoch, 1u, tf, tv);
+      constexpr int LB = 4;
+      int64_t k0 = 0;
+      bool gave_up = false;
+      while (true) {
+        uint32_t fl[LB];
+        bool en[LB];
+        S v[LB];
+#pragma unroll
+        for (int i = 0; i < LB; ++i) {
+          const int64_t pt = tile - 1 - (k0 + lane * LB + i);
+          fl[i] = pt >= 0 ? 0u : 2u;
+          en[i] = pt < 0;
+          v[i] = A::id();
+        }
+        uint32_t it = 0;
+        while (true) {
+          bool ready = true;
+#pragma unroll
+          for (int i = 0; i < LB; ++i) {
+            if (fl[i] == 0) fl[i] = peek_seg<S>(a.status, tile - 1 - (k0 + lane * LB + i), a.epoch, v[i], en[i]);
+            ready = ready && fl[i] != 0;
+          }
+          if (__all_sync(0xffffffffu, ready)) break;
+          ++it;
+          const bool stop = gave_up || it > SPIN_LIMIT ||
+                            ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
+          if (__any_sync(0xffffffffu, stop)) {
+            gave_up = true;
+            if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
+#pragma unroll
+            for (int i = 0; i < LB; ++i)
+              if (fl[i] == 0) { fl[i] = 2u; en[i] = true; }
+            break;
+          }
+          __nanosleep(it < 8 ? 32 : 128);
+        }
+        // Nearest-first fold, stopping at an inclusive prefix or a tile that
+        // holds a segment end (its value already starts after that end).
+        bool stop_here = false;
+        S lv = A::id();
+#pragma unroll
+        for (int i = 0; i < LB; ++i) {
+          if (!stop_here) lv = A::comb(v[i], lv);
+          stop_here = stop_here || fl[i] == 2u || en[i];
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, stop_here);
+        const int kp = pm ? __ffs(pm) - 1 : 32;
+        if (lane > kp) lv = A::id();
+        S wr = warp_reduce_rev<A>(lv);
+        wr = shfl_idx(wr, 0);
+        carry = A::comb(wr, carry);
+        if (pm) break;
+        k0 += 32 * LB;
+      }
+      // Inclusive value at the tile end: what the next tile carries in.
+      if (lane == 0) publish_seg<S>(a.status, tile, a.epoch, 2u, true, tf ? tv : A::comb(carry, tv));
+    } else if (lane == 0) {
+      publish_seg<S>(a.status, tile, a.epoch, 2u, true, tv);
+    }
+    if (lane == 0) s_carry = carry;
+  }
+  __syncthreads();
+
+  // ---- pass 2: walk the row again from its carried-in value, writing segments
+  S run;
+  {
+    // value carried into this row: (tile carry) . (warps before) . (lanes before)
+    S c = s_carry;
+    c = wf ? wv : A::comb(c, wv);
+    run = exf ? ex : A::comb(c, ex);
+  }
+  {
+    T x[ITEMS];
+    load_row(x);
+    T *out = static_cast<T *>(a.out);
+    const T z = from_bits<T>(a.seed);
+    int64_t i = i0;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      run = A::push(run, x[j]);
+      if ((emask >> j) & 1u) {
+        // The first end of a run of equal ends closes a non-empty segment,
+        // except segment 0 when it is empty (a tile starting before off[0]).
+        if (a.has_seed || lo + i != 0 || seg_off2(a, 0) < seg_off2(a, 1))
+          out[lo + i] = A::lower(a.has_seed ? A::comb(A::lift(z), run) : run);
+        run = A::id();
+        const int e = r0 + j + 1;
+        do { ++i; } while (end_at(i) == e);
+      }
+    }
+  }
+}
+
+template <int OP, class T, int PREC>
+int foldseg_scan_typed(Workspace *w, const T *in, const void *off, int off64, T *out, int64_t inner,
+                       int64_t nseg, bool has_seed, uint64_t seed, cudaStream_t s, bool *taken) {
+  constexpr int ITEMS = FS_ROW_BYTES / sizeof(T);
+  constexpr int64_t TE = (int64_t)FS_THREADS * ITEMS;
+  *taken = false;
+  const int64_t full_rows = inner / ITEMS;
+  CUtensorMap tin;
+  memset(&tin, 0, sizeof(tin));
+  if (full_rows == 0 || !encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, FS_ROW_BYTES, ITEMS, FS_THREADS, true))
+    return ACC_OK;  // not describable by TMA: the caller uses the per-segment kernels
+  const int64_t ntiles = cdiv_h(inner, TE);
+  if (ntiles >= (1ll << 31)) return ACC_OK;
+  *taken = true;
+  int st = ws_status(w, (size_t)ntiles * 2);
+  if (st) return st;
+  st = ws_scratch(w, (size_t)ntiles * sizeof(int64_t) + 256);
+  if (st) return st;
+  SegScanArgs a{};
+  a.in = in; a.off = off; a.out = out;
+  a.inner = inner; a.nseg = nseg; a.off64 = off64;
+  a.seed = seed; a.has_seed = has_seed;
+  a.full_rows = full_rows; a.ntiles = ntiles;
+  a.tile_seg = static_cast<int64_t *>(w->scratch);
+  a.status = w->status;
+  a.ticket = w->words + W_TICKET;
+  a.err = w->words + W_ERR;
+  a.epoch = ws_next_epoch(w, s);
+  cudaError_t e = cudaMemsetAsync(a.tile_seg, 0xff, (size_t)ntiles * sizeof(int64_t), s);
+  if (e != cudaSuccess) return cuda_status(e);
+  const Device &d = device_info();
+  int64_t pb = cdiv_h(nseg, 256);
+  if (pb > (int64_t)d.sms * 8) pb = (int64_t)d.sms * 8;
+  if (pb < 1) pb = 1;
+  seg_tiles_kernel<T><<<(unsigned)pb, 256, 0, s>>>(a, TE);
+  st = check_launch();
+  if (st) return st;
+  const size_t smem = (size_t)FS_THREADS * FS_ROW_BYTES + 1024;
+  auto kern = foldseg_scan_kernel<OP, T, PREC>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    attr = true;
+  }
+  kern<<<(unsigned)ntiles, FS_THREADS, smem, s>>>(tin, a);
+  return check_launch();
+}
+
 // ----------------------------------------------------------------- host side
 template <int OP, class T, int PREC>
 int foldseg_typed(Workspace *w, const T *in, const void *off, int off64, T *out, int64_t outer,
@@ -220,6 +601,16 @@ int foldseg_dispatch(Workspace *w, int op, int type, int prec, const void *in, c
       constexpr int OP = decltype(opc)::value;
       return with_prec<OP, T>(prec, [&](auto pc) -> int {
         constexpr int P = decltype(pc)::value;
+        // The segmented single-pass kernel is opt-in (ACC_GB300_FOLDSEG=scan):
+        // on GB300 it is still slower than the per-segment kernels.
+        static const bool seg_scan = getenv("ACC_GB300_FOLDSEG") && strcmp(getenv("ACC_GB300_FOLDSEG"), "scan") == 0;
+        if (outer == 1 && seg_scan) {
+          bool taken = false;
+          const int st = foldseg_scan_typed<OP, T, P>(w, static_cast<const T *>(in), off, off64,
+                                                      static_cast<T *>(out), inner, nseg, seed != nullptr, sb, s,
+                                                      &taken);
+          if (taken || st) return st;
+        }
         return foldseg_typed<OP, T, P>(w, static_cast<const T *>(in), off, off64, static_cast<T *>(out),
                                        outer, inner, nseg, seed != nullptr, sb, s);
       });

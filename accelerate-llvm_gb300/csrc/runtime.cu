@@ -117,10 +117,11 @@ int ws_scratch(Workspace *w, size_t bytes) {
 }
 
 uint32_t ws_next_epoch(Workspace *w, cudaStream_t s) {
-  // Epochs live in 30 bits of the status tag.  On wrap-around the slots are
-  // cleared so that no stale tag can ever match.
+  // Epochs live in 29 bits of the status tag (the segmented scan of foldSeg
+  // uses one more tag bit).  On wrap-around the slots are cleared so that no
+  // stale tag can ever match.
   w->epoch += 1;
-  if (w->epoch >= (1u << 30)) {
+  if (w->epoch >= (1u << 29)) {
     cudaMemsetAsync(w->status, 0, w->nstatus * sizeof(uint64_t), s);
     w->epoch = 1;
   }

@@ -11,6 +11,7 @@ seeded synthetic data of the workload's shapes and distributions, generated
 on the device; every input is larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --only scan|fold|permute|stencil|foldseg [--scale S]   (one kernel, small case)
 
 `--impl reference` times the CPU restatement of accelerate-llvm-native (the
 reference's own CPU backend cannot be built here) on all host cores over a
@@ -44,9 +45,18 @@ BYTES = {
     "permute": 4 * N_PERM + 2 * 4 * M_PERM,
     "stencil": 8 * H_ST * W_ST,
 }
-# DRAM bytes per launch from one ncu capture of each kernel (dram__bytes_read.sum
-# + dram__bytes_write.sum), scaled to the full launch; see profiles/.
-NCU_TRAFFIC = {"scan": None}
+# DRAM bytes per launch of the scan kernel: dram__bytes_read.sum +
+# dram__bytes_write.sum of one ncu capture at 2^25 Int64 elements
+# (268.6 MB + 212.0 MB; profiles/scan_tma_kernel_int64.md), scaled by the
+# element count to the 2^28 launch (traffic grows in proportion).
+NCU_TRAFFIC = {"scan": int((268.6e6 + 212.0e6) * 8)}
+
+# foldSeg workload: 2^26 Float32 values ~ N(0,1) in 2^20 segments with
+# lognormal lengths (median 48, sigma 1.5, capped at 2^16, 2 % empty),
+# rescaled by largest remainder so that the lengths sum to 2^26; plus Int32
+# `max` over the same segmentation.  Bytes: values + offsets + results.
+N_SEG_VALUES, N_SEGS = 1 << 26, 1 << 20
+BYTES_FOLDSEG = 4 * N_SEG_VALUES + 4 * (N_SEGS + 1) + 4 * N_SEGS
 
 
 def peaks():
@@ -73,7 +83,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -131,6 +141,26 @@ def make_inputs(torch, dev, scale=1):
         del u, r
     grid = torch.rand((h, h), dtype=torch.float32, device=dev, generator=g)
     return {"scan": x_scan, "fold": x_fold, "idx": idx, "grid": grid}
+
+
+def make_segments(torch, dev, n_values=N_SEG_VALUES, nseg=N_SEGS):
+    """Lognormal(median 48, sigma 1.5) lengths capped at 2^16 with 2 % empty,
+    rescaled by largest remainder to sum to n_values; returns Int32 offsets."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 3)
+    lens = torch.empty(nseg, dtype=torch.float64, device=dev).log_normal_(float(np.log(48.0)), 1.5, generator=g)
+    lens.clamp_(max=float(1 << 16))
+    lens[torch.rand(nseg, device=dev, generator=g) < 0.02] = 0.0
+    lens *= n_values / lens.sum()
+    fl = torch.floor(lens)
+    rem = int(n_values - int(fl.sum().item()))
+    order = torch.argsort(lens - fl, descending=True)
+    fl[order[:rem]] += 1.0
+    off = torch.zeros(nseg + 1, dtype=torch.int64, device=dev)
+    off[1:] = torch.cumsum(fl.to(torch.int64), 0)
+    vals = torch.randn(n_values, dtype=torch.float32, device=dev, generator=g)
+    ivals = torch.randint(-(1 << 31), (1 << 31) - 1, (n_values,), dtype=torch.int32, device=dev, generator=g)
+    return off.to(torch.int32), vals, ivals
 
 
 W9 = [[1.0 / 9] * 3] * 3
@@ -196,6 +226,11 @@ def run_ours(args, rank, world):
     assert int(outs["permute"].sum().item()) == N_PERM
     assert int(outs["scan"][-1].item()) == int(inp["scan"].sum().item())
 
+    # ---- foldSeg and batched workloads (reported beside the metric, not part of `value`)
+    extra = {"foldseg": run_foldseg(torch, acc, args, dev)}
+    if not args.no_batch:
+        extra["batched"] = run_batched(torch, acc, args, dev)
+
     # ---- end to end through the public API with host buffers
     e2e = run_e2e(torch, acc, inp, zeros, args, dev)
 
@@ -228,7 +263,8 @@ def run_ours(args, rank, world):
                                "Zipf(1.1) -> 2^16 bins; stencil 3x3 Float32 8192^2 clamp",
                    "l2": "every input > L2 (129 MB); no flush", "parallelism": f"replicas x{world}"},
         "per_skeleton": per_sk,
-        "roofline": {"bound": "hbm", "kernel": "scan_lookback_kernel (scanl1 + Int64)", "achieved": round(achieved, 1),
+        "extra": extra,
+        "roofline": {"bound": "hbm", "kernel": "scan_tma_kernel (scanl1 + Int64)", "achieved": round(achieved, 1),
                      "peak": peak, "peak_kind": f"{peak_kind} hbm_gbs (copy)", "unit": "GB/s",
                      "frac": round(achieved / peak, 3),
                      "traffic": NCU_TRAFFIC["scan"]},
@@ -241,11 +277,160 @@ def run_ours(args, rank, world):
     return line
 
 
-def run_e2e(torch, acc, inp, zeros, args, dev):
-    """Same step through the public API with pinned host inputs: H2D copy of
-    every input, the four skeletons, D2H of every result, per step."""
-    host = {k: v.cpu().pin_memory() for k, v in inp.items()}
+def run_foldseg(torch, acc, args, dev):
+    """foldSeg (+) Float32 compensated, plain and FP64-accumulated, and foldSeg max Int32, on the lognormal
+    segmentation; device time per call and HBM GB/s (values + offsets + results)."""
+    off, vals, ivals = make_segments(torch, dev)
+    peak, _ = peaks()
     stream = torch.cuda.current_stream()
+    res = {}
+    runs = {"f32_add_compensated": lambda: acc.fold_seg("+", 0.0, vals, off),
+            "f32_add_plain": lambda: acc.fold_seg("+", 0.0, vals, off, prec="plain"),
+            "f32_add_fp64acc": lambda: acc.fold_seg("+", 0.0, vals, off, prec="fp64"),
+            "i32_max": lambda: acc.fold_seg("max", -(1 << 31), ivals, off)}
+    for name, fn in runs.items():
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = BYTES_FOLDSEG / (ms * 1e-3) / 1e9
+        res[name] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
+    acc.sync()
+    res["workload"] = "foldSeg over 2^26 values in 2^20 lognormal segments (median 48, sigma 1.5, 2% empty)"
+    return res
+
+
+def run_batched(torch, acc, args, dev, count=10_000):
+    """10,000 independent requests, a quarter each of fold (+) and scanl1 (+)
+    on Int32 and on Float32, sizes log-uniform in [2^8, 2^22]: one persistent
+    launch replayed as a CUDA graph (tiles from the autotuner) against the
+    same requests as 10,000 per-call launches."""
+    rng = np.random.default_rng(SEED + 4)
+    sizes = np.exp(rng.uniform(np.log(2 ** 8), np.log(2 ** 22), size=count)).astype(np.int64)
+    kinds = ["fold", "scan", "fold", "scan"] * (count // 4)
+    dts = [torch.int32, torch.int32, torch.float32, torch.float32] * (count // 4)
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 5)
+    tot = {torch.int32: 0, torch.float32: 0}
+    for n, dt in zip(sizes, dts):
+        tot[dt] += int(n)
+    pool = {torch.int32: torch.randint(-1000, 1000, (tot[torch.int32],), dtype=torch.int32, device=dev, generator=g),
+            torch.float32: torch.randn(tot[torch.float32], dtype=torch.float32, device=dev, generator=g)}
+    at = {torch.int32: 0, torch.float32: 0}
+    reqs, nbytes = [], 0
+    for n, dt, kind in zip(sizes, dts, kinds):
+        n = int(n)
+        xs = pool[dt][at[dt]:at[dt] + n]
+        at[dt] += n
+        out = torch.empty((1,) if kind == "fold" else (n,), dtype=dt, device=dev)
+        reqs.append((kind, xs, out, 0 if kind == "fold" else None))
+        nbytes += 4 * n if kind == "fold" else 8 * n
+    table = ROOT / "accelerate-llvm_gb300" / "_build" / "batch_tuning.json"
+    t_tune = time.perf_counter()
+    if table.exists():
+        acc.batch_load_tuning(table)
+        tuned = "loaded"
+    else:
+        table.parent.mkdir(exist_ok=True)
+        acc.batch_autotune(str(table))
+        tuned = "autotuned"
+    t_tune = time.perf_counter() - t_tune
+    b = acc.Batch("+", reqs)
+    b.capture()
+    stream = torch.cuda.current_stream()
+    for _ in range(max(1, args.warmup)):
+        b.launch()
+    b.status()
+    reps = max(3, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.launch()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    b.status()
+    ms_batch = e0.elapsed_time(e1) / reps
+    batched_out = [r[2].clone() for r in reqs[:8]]
+    b.close()
+
+    def per_call():
+        for kind, xs, out, z in reqs:
+            if kind == "fold":
+                acc.fold("+", z, xs)
+            else:
+                acc.scanl1("+", xs)
+
+    per_call()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    e0.record(stream)
+    per_call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_call = max(e0.elapsed_time(e1), (time.perf_counter() - w0) * 1e3)
+    acc.sync()
+    for (kind, xs, out, z), got in zip(reqs[:8], batched_out):
+        ref = acc.fold("+", z, xs).reshape(1) if kind == "fold" else acc.scanl1("+", xs)
+        if xs.dtype == torch.int32:
+            assert torch.equal(got, ref)
+    return {"requests": count, "bytes": nbytes, "tiles": tuned, "tune_s": round(t_tune, 2),
+            "batched_graph": {"ms": round(ms_batch, 3), "req_per_s": round(count / (ms_batch * 1e-3)),
+                              "gbs": round(nbytes / (ms_batch * 1e-3) / 1e9, 1)},
+            "per_call": {"ms": round(ms_call, 3), "req_per_s": round(count / (ms_call * 1e-3)),
+                         "gbs": round(nbytes / (ms_call * 1e-3) / 1e9, 1)},
+            "speedup": round(ms_call / ms_batch, 2)}
+
+
+def run_only(args):
+    """One skeleton at 1/scale of its full size, `--steps` launches: the
+    small-case command used for ncu captures."""
+    import torch
+    import __graft_entry__ as ge
+    dev = torch.device("cuda", 0)
+    acc = ge.load_package()
+    acc.load()
+    name = args.only
+    stream = torch.cuda.current_stream()
+    if name == "foldseg":
+        off, vals, ivals = make_segments(torch, dev, N_SEG_VALUES // args.scale, N_SEGS // args.scale)
+        fn, nbytes = (lambda: acc.fold_seg("+", 0.0, vals, off)), BYTES_FOLDSEG // args.scale
+    else:
+        inp = make_inputs(torch, dev, args.scale)
+        zeros = torch.zeros(M_PERM, dtype=torch.int32, device=dev)
+        fn = {"scan": lambda: acc.scanl1("+", inp["scan"]), "fold": lambda: acc.fold("+", 0.0, inp["fold"]),
+              "permute": lambda: acc.permute("+", zeros, inp["idx"], 1),
+              "stencil": lambda: acc.stencil(W9, inp["grid"], "clamp")}[name]
+        h = inp["grid"].shape[0]
+        nbytes = {"scan": 16 * inp["scan"].numel(), "fold": 4 * inp["fold"].numel(),
+                  "permute": 4 * inp["idx"].numel() + 8 * M_PERM, "stencil": 8 * h * h}[name]
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    acc.sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    return {"only": name, "scale": args.scale, "ms": round(ms, 4), "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1)}
+
+
+def run_e2e(torch, acc, inp, zeros, args, dev):
+    """Same step through the public API with host buffers: every step copies
+    each input from pinned host memory, runs the four skeletons and copies
+    every result back.  Copies in, kernels and copies out run on three streams
+    ordered by events, skeleton by skeleton (scan first, so that its 2 GiB
+    result drains while the other inputs upload)."""
+    host = {k: v.cpu().pin_memory() for k, v in inp.items()}
+    order = [("scan", "scan"), ("fold", "fold"), ("permute", "idx"), ("stencil", "grid")]
     h2d = sum(v.numel() * v.element_size() for v in host.values())
     res_host = {
         "scan": torch.empty(N_SCAN, dtype=torch.int64).pin_memory(),
@@ -255,15 +440,33 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
     }
     d2h = sum(v.numel() * v.element_size() for v in res_host.values())
     dev_in = {k: torch.empty_like(v, device=dev) for k, v in host.items()}
+    s_in, s_run, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
 
     def step():
-        for k in host:
-            dev_in[k].copy_(host[k], non_blocking=True)
-        outs = {"scan": acc.scanl1("+", dev_in["scan"]), "fold": acc.fold("+", 0.0, dev_in["fold"]),
-                "permute": acc.permute("+", zeros, dev_in["idx"], 1),
-                "stencil": acc.stencil(W9, dev_in["grid"], "clamp")}
-        for k, v in outs.items():
-            res_host[k].copy_(v, non_blocking=True)
+        for name, key in order:
+            with torch.cuda.stream(s_in):
+                dev_in[key].copy_(host[key], non_blocking=True)
+                ready = torch.cuda.Event()
+                ready.record(s_in)
+            s_run.wait_event(ready)
+            with torch.cuda.stream(s_run):
+                if name == "scan":
+                    out = acc.scanl1("+", dev_in["scan"], stream=s_run)
+                elif name == "fold":
+                    out = acc.fold("+", 0.0, dev_in["fold"], stream=s_run)
+                elif name == "permute":
+                    out = acc.permute("+", zeros, dev_in["idx"], 1, stream=s_run)
+                else:
+                    out = acc.stencil(W9, dev_in["grid"], "clamp", stream=s_run)
+                done = torch.cuda.Event()
+                done.record(s_run)
+                # the input buffer is reused next step only after this kernel
+                dev_in[key].record_stream(s_run)
+            s_out.wait_event(done)
+            with torch.cuda.stream(s_out):
+                res_host[name].copy_(out, non_blocking=True)
+                out.record_stream(s_out)
+            s_in.wait_event(done)  # next step's upload of this input waits for its consumer
 
     for _ in range(max(1, args.warmup // 2)):
         step()
@@ -271,16 +474,21 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
     steps = max(2, args.steps // 2)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
+    t0.record(s_in)
+    s_run.wait_event(t0)
+    s_out.wait_event(t0)
     for _ in range(steps):
         step()
-    t1.record(stream)
+    s_out.wait_stream(s_in)
+    s_out.wait_stream(s_run)
+    t1.record(s_out)
     torch.cuda.synchronize()
-    acc.sync()
+    acc.sync(s_run)
     ms = t0.elapsed_time(t1) / steps
     del dev_in
     return {"value": round(sum(BYTES.values()) / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "ms_per_step": round(ms, 3),
-            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "path": "C ABI through the Python host layer; pinned host buffers; H2D / kernels / D2H on three streams"}
 
 
 # ----------------------------------------------------------------- CPU arm
@@ -393,12 +601,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-scale", type=int, default=4, help="CPU sample = 1/scale of each input")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch workload")
+    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg"],
+                    help="time one skeleton alone (small-case driver for ncu captures)")
+    ap.add_argument("--scale", type=int, default=1, help="with --only: 1/scale of the full input")
     args = ap.parse_args()
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         if rank != 0:
             return
         print(json.dumps(run_reference(args)))
+        return
+    if args.only:
+        print(json.dumps(run_only(args)))
         return
     rank, world = dist_init()
     line = run_ours(args, rank, world)

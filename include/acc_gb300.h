@@ -256,6 +256,62 @@ int acc_stencil2d_pair(int type, int ry, int rx, const void *wa_w,
                        int64_t ha, int64_t wa, const void *b, int64_t hb,
                        int64_t wb, void *out, void *stream);
 
+/* ---------------------------------------------------------------- batches */
+
+/* Many independent fold / scanl1 requests in ONE persistent kernel launch.
+ * No counterpart in the reference, which launches every skeleton separately
+ * (PTX/Execute.hs:835-881); this is the batched execution the benchmark spec
+ * asks for.  A request is fold z xs / fold1 xs (one output element) or
+ * scanl1 xs (n outputs; with a seed, the seed is combined on the left of
+ * every prefix) over one contiguous vector, element type ACC_I32 / ACC_I64 /
+ * ACC_F32 / ACC_F64; every request of a batch uses the same primitive, one
+ * of ACC_ADD / ACC_MIN / ACC_MAX (Float32 + is compensated). */
+typedef enum acc_request_kind { ACC_REQ_FOLD = 0, ACC_REQ_SCAN = 1 } acc_request_kind;
+
+typedef struct acc_request {
+  int kind;          /* acc_request_kind                                   */
+  int type;          /* acc_type                                           */
+  const void *in;    /* n elements (device)                                */
+  void *out;         /* fold: 1 element; scan: n elements (device)         */
+  int64_t n;
+  int has_seed;      /* 0: fold1 / scanl1 without seed                     */
+  uint64_t seed;     /* seed bits in the element type (low bytes)          */
+} acc_request;
+
+typedef struct acc_batch acc_batch;  /* opaque plan */
+
+/* Plan a batch: validates the requests, cuts each into tiles whose size
+ * comes from the autotuner table (acc_batch_autotune / acc_batch_load_tuning;
+ * built-in defaults otherwise) and allocates every scratch array the launch
+ * will need.  The requests' buffers must stay valid while the plan is used. */
+int acc_batch_create(int op, const acc_request *reqs, int64_t count,
+                     acc_batch **out);
+
+/* Capture the batch's launch into a CUDA graph once; later acc_batch_launch
+ * calls replay the graph. */
+int acc_batch_capture(acc_batch *batch, void *stream);
+
+/* Run every request of the batch: one persistent kernel (or one replay of the
+ * captured graph).  Stream-ordered; allocates nothing. */
+int acc_batch_launch(acc_batch *batch, void *stream);
+
+/* Synchronise `stream` and report a device-side failure of the batch
+ * (ACC_ERR_TIMEOUT if a bounded look-back wait ran out). */
+int acc_batch_status(acc_batch *batch, void *stream);
+
+/* Free the plan (waits for the device first). */
+int acc_batch_destroy(acc_batch *batch);
+
+/* Autotuner: for fold and scan, Int32 / Float32 / Int64 / Float64 and every
+ * size bucket 2^8 .. 2^22, time one batched launch per candidate tile size
+ * (256 x 1, 2, 4, ... elements) and keep the fastest; the table is used by
+ * later acc_batch_create calls and written as JSON to `table_path` (NULL:
+ * not written). */
+int acc_batch_autotune(const char *table_path, void *stream);
+
+/* Load a table written by acc_batch_autotune. */
+int acc_batch_load_tuning(const char *table_path);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,6 +90,7 @@ SIGNATURES = {
     "acc_batch_destroy": ([_P], _I),
     "acc_batch_autotune": ([ctypes.c_char_p, _P], _I),
     "acc_batch_load_tuning": ([ctypes.c_char_p], _I),
+    "acc_serve_run": ([_P, _L, _L, _I, _I, _P, _P], _I),
 }
 
 
@@ -413,3 +414,46 @@ def batch_autotune(table_path=None, stream=None):
 
 def batch_load_tuning(table_path):
     _check(lib().acc_batch_load_tuning(str(table_path).encode()), "load tuning")
+
+
+# ----------------------------------------------------------------- serving
+SK_FOLD, SK_SCAN, SK_FOLDSEG, SK_PERMUTE, SK_STENCIL = range(5)
+SKELETONS = {"fold": SK_FOLD, "scan": SK_SCAN, "foldseg": SK_FOLDSEG, "permute": SK_PERMUTE, "stencil": SK_STENCIL}
+
+
+class ServeReq(ctypes.Structure):
+    """struct acc_serve_req of acc_gb300.h."""
+    _fields_ = [("skeleton", ctypes.c_int), ("type", ctypes.c_int), ("inp", ctypes.c_void_p),
+                ("aux", ctypes.c_void_p), ("out", ctypes.c_void_p), ("n", ctypes.c_int64), ("m", ctypes.c_int64),
+                ("arrival", ctypes.c_double)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("wall_s", ctypes.c_double), ("served", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("max_inflight", ctypes.c_int64), ("peak_bytes", ctypes.c_int64)]
+
+
+def serve(requests, budget_bytes: int, slots: int = 8, mode: str = "batching"):
+    """Serve a request stream (acc_serve_run).  `requests`: list of
+    (skeleton name, input tensor, aux tensor or None, output tensor, n, m,
+    arrival seconds), sorted by arrival.  Returns (latencies in seconds as a
+    list, stats dict)."""
+    arr = (ServeReq * max(1, len(requests)))()
+    keep = []
+    for i, (sk, xs, aux, out, n, m, t) in enumerate(requests):
+        keep += [xs, aux, out]
+        arr[i].skeleton = SKELETONS[sk]
+        arr[i].type = type_of(xs) if sk != "permute" else I32
+        arr[i].inp = xs.data_ptr()
+        arr[i].aux = aux.data_ptr() if aux is not None else 0
+        arr[i].out = out.data_ptr()
+        arr[i].n = n
+        arr[i].m = m
+        arr[i].arrival = t
+    lat = (ctypes.c_double * max(1, len(requests)))()
+    stats = ServeStats()
+    st = lib().acc_serve_run(ctypes.cast(arr, ctypes.c_void_p), len(requests), int(budget_bytes), slots,
+                             0 if mode == "batching" else 1, ctypes.cast(lat, ctypes.c_void_p),
+                             ctypes.cast(ctypes.pointer(stats), ctypes.c_void_p))
+    _check(st, "acc_serve_run")
+    return list(lat)[:len(requests)], {k: getattr(stats, k) for k, _ in ServeStats._fields_}

@@ -124,9 +124,12 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
   const int64_t tail0 = head + nvec * VEC;
   if (tail0 + threadIdx.x < len) acc = A::push(acc, src[tail0 + threadIdx.x]);
   acc = b_block_reduce<A>(acc, s_part);
-  S *parts = reinterpret_cast<S *>(a.partials);
+  // One 8-byte slot per item whatever the state's size, so that requests of
+  // different types in one batch never share partial slots.
+  static_assert(sizeof(S) <= sizeof(uint64_t), "fold state larger than a partial slot");
+  auto part = [&](int64_t it) { return reinterpret_cast<S *>(a.partials + it); };
   if (threadIdx.x == 0) {
-    parts[item] = acc;
+    *part(item) = acc;
     __threadfence();
     const uint32_t prev = atomicAdd(a.req_ticket + r, 1u);
     s_last = prev == (uint32_t)(q.ntiles - 1);
@@ -137,7 +140,7 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
     S v = A::id();
     const int64_t per = (q.ntiles + BT - 1) / BT;
     const int64_t lo = threadIdx.x * per, hi = lo + per < q.ntiles ? lo + per : q.ntiles;
-    for (int64_t i = lo; i < hi; ++i) v = A::comb(v, ld_state<S>(&parts[q.first_item + i]));
+    for (int64_t i = lo; i < hi; ++i) v = A::comb(v, ld_state<S>(part(q.first_item + i)));
     v = b_block_reduce<A>(v, s_part);
     if (threadIdx.x == 0) {
       if (q.has_seed) v = A::comb(A::lift(from_bits<T>(q.seed)), v);
@@ -421,6 +424,112 @@ static int batch_make(int op, const acc_request *reqs, int64_t count, const int3
   if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
   *out = b;
   return ACC_OK;
+}
+
+// ---------------------------------------------------------------- arena
+// A reusable launch area for batches assembled on the fly (the serving
+// loop): device arrays sized once for up to cap_reqs requests / cap_items
+// tiles, pinned host staging for the descriptors.  A launch copies the new
+// descriptors with cudaMemcpyAsync and runs the kernel; it allocates nothing.
+// One arena serves one stream at a time: its staging buffers are reused only
+// after the previous launch from the arena has completed.
+struct BatchArena {
+  Batch dev;            // device arrays and launch shape (count/nitems per launch)
+  int64_t cap_reqs = 0, cap_items = 0;
+  BReq *h_reqs = nullptr;
+  int32_t *h_item = nullptr;
+};
+
+int arena_create(int op, int64_t cap_reqs, int64_t cap_items, BatchArena **out) {
+  if (op != ACC_ADD && op != ACC_MIN && op != ACC_MAX) return ACC_ERR_UNSUPPORTED;
+  BatchArena *ar = new BatchArena();
+  Batch *b = &ar->dev;
+  b->op = op;
+  cudaGetDevice(&b->device);
+  ar->cap_reqs = cap_reqs;
+  ar->cap_items = cap_items;
+  cudaError_t e;
+  if ((e = cudaMalloc(&b->d_reqs, sizeof(BReq) * cap_reqs)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_item_req, sizeof(int32_t) * cap_items)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_status, sizeof(uint64_t) * 2 * cap_items)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_partials, sizeof(uint64_t) * cap_items)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_req_ticket, sizeof(uint32_t) * cap_reqs)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_words, sizeof(uint32_t) * 64)) != cudaSuccess ||
+      (e = cudaMallocHost(&ar->h_reqs, sizeof(BReq) * cap_reqs)) != cudaSuccess ||
+      (e = cudaMallocHost(&ar->h_item, sizeof(int32_t) * cap_items)) != cudaSuccess) {
+    arena_free(ar);
+    return cuda_status(e);
+  }
+  cudaMemset(b->d_status, 0, sizeof(uint64_t) * 2 * cap_items);
+  cudaMemset(b->d_req_ticket, 0, sizeof(uint32_t) * cap_reqs);
+  cudaMemset(b->d_words, 0, sizeof(uint32_t) * 64);
+  b->smem = (size_t)B_MAX_TILE_BYTES + BT * 8 + 256;
+  void *kern = op == ACC_ADD ? batch_kernel_ptr<ACC_ADD>() : op == ACC_MIN ? batch_kernel_ptr<ACC_MIN>()
+                                                                          : batch_kernel_ptr<ACC_MAX>();
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, b->smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  b->grid = device_info().sms * per_sm;
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { arena_free(ar); return cuda_status(e); }
+  *out = ar;
+  return ACC_OK;
+}
+
+// Tiles a request will take (0 if it does not fit the batch kernel).
+int64_t arena_tiles(const acc_request &q) {
+  const int ipt = std::min(std::max(tuned_ipt(q.kind, q.type, q.n), 1), max_ipt(q.type));
+  const int64_t ts = (int64_t)ipt * BT;
+  const int64_t nt = (q.n + ts - 1) / ts;
+  return (q.kind == ACC_REQ_FOLD && nt == 0) ? 1 : nt;
+}
+
+int arena_launch(BatchArena *ar, const acc_request *reqs, int64_t count, cudaStream_t s) {
+  Batch *b = &ar->dev;
+  int64_t nitems = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const acc_request &q = reqs[i];
+    int ipt = std::min(std::max(tuned_ipt(q.kind, q.type, q.n), 1), max_ipt(q.type));
+    const int64_t ts = (int64_t)ipt * BT;
+    int64_t nt = (q.n + ts - 1) / ts;
+    if (q.kind == ACC_REQ_FOLD && nt == 0) nt = 1;
+    if (i >= ar->cap_reqs || nitems + nt > ar->cap_items) return ACC_ERR_TOO_LARGE;
+    BReq &r = ar->h_reqs[i];
+    r.in = q.in; r.out = q.out; r.n = q.n; r.seed = q.seed;
+    r.kind = q.kind; r.type = q.type; r.has_seed = q.has_seed; r.ipt = ipt;
+    r.first_item = nitems; r.ntiles = nt;
+    for (int64_t k = 0; k < nt; ++k) ar->h_item[nitems + k] = (int32_t)i;
+    nitems += nt;
+  }
+  if (nitems == 0) return ACC_OK;
+  cudaError_t e = cudaMemcpyAsync(b->d_reqs, ar->h_reqs, sizeof(BReq) * count, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->d_item_req, ar->h_item, sizeof(int32_t) * nitems, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_status(e);
+  b->count = count;
+  b->nitems = nitems;
+  const int full_grid = b->grid;
+  if (b->grid > nitems) b->grid = (int)nitems;
+  const int st = batch_launch_raw(b, s);
+  b->grid = full_grid;
+  return st;
+}
+
+void arena_free(BatchArena *ar) {
+  if (!ar) return;
+  Batch *b = &ar->dev;
+  cudaFree(b->d_reqs);
+  cudaFree(b->d_item_req);
+  cudaFree(b->d_status);
+  cudaFree(b->d_partials);
+  cudaFree(b->d_req_ticket);
+  cudaFree(b->d_words);
+  cudaFreeHost(ar->h_reqs);
+  cudaFreeHost(ar->h_item);
+  delete ar;
 }
 
 // ---------------------------------------------------------------- autotune

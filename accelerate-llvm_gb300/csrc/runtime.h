@@ -127,6 +127,13 @@ inline int64_t cdiv_h(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // the reference's `generate` of the seed, PTX/CodeGen/Generate.hs:40-61).
 template <class T> int launch_fill(T *out, int64_t n, uint64_t bits, cudaStream_t s);
 
+// Reusable batch launch area (batch.cu), used by the serving loop.
+struct BatchArena;
+int arena_create(int op, int64_t cap_reqs, int64_t cap_items, BatchArena **out);
+int64_t arena_tiles(const acc_request &q);
+int arena_launch(BatchArena *ar, const acc_request *reqs, int64_t count, cudaStream_t s);
+void arena_free(BatchArena *ar);
+
 // Exclusive `scanl (+) 0` of nseg segment lengths into nseg+1 offsets.
 int scan_offsets(Workspace *w, int type, const void *lengths, void *offsets, int64_t nseg, cudaStream_t s);
 

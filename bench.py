@@ -230,6 +230,8 @@ def run_ours(args, rank, world):
     extra = {"foldseg": run_foldseg(torch, acc, args, dev)}
     if not args.no_batch:
         extra["batched"] = run_batched(torch, acc, args, dev)
+    if args.serve_seconds > 0:
+        extra["serving"] = run_serving(torch, acc, args, dev)
 
     # ---- end to end through the public API with host buffers
     e2e = run_e2e(torch, acc, inp, zeros, args, dev)
@@ -385,6 +387,76 @@ def run_batched(torch, acc, args, dev, count=10_000):
             "per_call": {"ms": round(ms_call, 3), "req_per_s": round(count / (ms_call * 1e-3)),
                          "gbs": round(nbytes / (ms_call * 1e-3) / 1e9, 1)},
             "speedup": round(ms_call / ms_batch, 2)}
+
+
+W5 = [[0.0, 0.25, 0.0], [0.25, -1.0, 0.25], [0.0, 0.25, 0.0]]
+
+
+def serving_stream(torch, dev, count, rate, rng, pools):
+    """Mixed requests: 40 % fold, 25 % scanl1, 15 % foldSeg (lognormal
+    segments), 10 % permute histograms into 2^12..2^16 bins, 10 % 5-point
+    Float32 stencils on 256^2..4096^2 grids; sizes log-uniform in
+    [2^10, 2^26]; Poisson arrivals at `rate` per second (rate 0: all at
+    t = 0).  Inputs are slices of device-resident pools; outputs rotate over
+    a pool of output regions."""
+    vals, ivals, off, idx, outs, offs_np = pools
+    kinds = rng.choice(["fold", "scan", "foldseg", "permute", "stencil"], size=count, p=[0.4, 0.25, 0.15, 0.1, 0.1])
+    sizes = np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 26), size=count)).astype(np.int64)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count)) if rate > 0 else np.zeros(count)
+    reqs = []
+    for i in range(count):
+        k, n = kinds[i], int(sizes[i])
+        out = outs[i % len(outs)]
+        if k in ("fold", "scan"):
+            xs = (vals if i % 2 else ivals)[:n]
+            reqs.append((k, xs, None, out.view(xs.dtype)[: (1 if k == "fold" else n)], n, 0, float(t[i])))
+        elif k == "foldseg":
+            nseg = int(np.searchsorted(offs_np, n, side="right")) - 1
+            nv = int(offs_np[nseg])
+            reqs.append((k, vals[:nv], off, out[:max(nseg, 1)], nv, nseg, float(t[i])))
+        elif k == "permute":
+            m = int(2 ** rng.integers(12, 17))
+            reqs.append((k, idx[m][:n], None, out.view(torch.int32)[:m], n, m, float(t[i])))
+        else:
+            side = int(np.exp(rng.uniform(np.log(256), np.log(4096))))
+            reqs.append((k, vals[:side * side].view(side, side), None, out[:side * side], side, side, float(t[i])))
+    return reqs
+
+
+def run_serving(torch, acc, args, dev):
+    """The serving stream at 20k req/s for --serve-seconds, through the
+    continuous-batching loop and through plain per-call launches; then each
+    scheduler's capacity with every request arriving at once."""
+    rng = np.random.default_rng(SEED + 6)
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 7)
+    n_pool = 1 << 26
+    vals = torch.randn(n_pool, dtype=torch.float32, device=dev, generator=g)
+    ivals = torch.randint(-1000, 1000, (n_pool,), dtype=torch.int32, device=dev, generator=g)
+    off, _, _ = make_segments(torch, dev, n_pool, 1 << 20)
+    idx = {m: torch.randint(0, m, (n_pool,), dtype=torch.int32, device=dev, generator=g) for m in [1 << b for b in range(12, 17)]}
+    outs = [torch.empty(n_pool, dtype=torch.float32, device=dev) for _ in range(64)]
+    pools = (vals, ivals, off, idx, outs, off.cpu().numpy().astype(np.int64))
+    budget = 40 << 30
+    res = {"rate_req_s": 20000, "seconds": args.serve_seconds, "budget_bytes": budget, "slots": 8}
+    count = int(20000 * args.serve_seconds)
+    stream = serving_stream(torch, dev, count, 20000.0, rng, pools)
+    for mode in ("batching", "per_call"):
+        lat, st = acc.serve(stream, budget, slots=8, mode=mode)
+        lat = np.array(lat)
+        res[mode] = {"served": st["served"], "wall_s": round(st["wall_s"], 3),
+                     "req_per_s": round(st["served"] / st["wall_s"]),
+                     "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                     "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
+                     "batches": st["batches"], "max_inflight": st["max_inflight"]}
+    cap_n = min(count, 20000)
+    burst = serving_stream(torch, dev, cap_n, 0.0, np.random.default_rng(SEED + 8), pools)
+    for mode in ("batching", "per_call"):
+        lat, st = acc.serve(burst, budget, slots=8, mode=mode)
+        res[mode]["capacity_req_s"] = round(st["served"] / st["wall_s"])
+    res["capacity_ratio"] = round(res["batching"]["capacity_req_s"] / res["per_call"]["capacity_req_s"], 2)
+    acc.sync()
+    return res
 
 
 def run_only(args):
@@ -602,6 +674,8 @@ def main():
     ap.add_argument("--cpu-scale", type=int, default=4, help="CPU sample = 1/scale of each input")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch workload")
+    ap.add_argument("--serve-seconds", type=float, default=3.0,
+                    help="length of the 20k req/s serving stream (0: skip serving)")
     ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg"],
                     help="time one skeleton alone (small-case driver for ncu captures)")
     ap.add_argument("--scale", type=int, default=1, help="with --only: 1/scale of the full input")

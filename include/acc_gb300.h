@@ -312,6 +312,53 @@ int acc_batch_autotune(const char *table_path, void *stream);
 /* Load a table written by acc_batch_autotune. */
 int acc_batch_load_tuning(const char *table_path);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A stream of mixed requests served by a continuous-batching loop (no
+ * counterpart in the reference).  Request semantics, all over device-resident
+ * arrays:
+ *   ACC_SK_FOLD     out[0] = fold (+) 0 in[0..n)
+ *   ACC_SK_SCAN     out = scanl1 (+) in[0..n)
+ *   ACC_SK_FOLDSEG  out[0..m) = foldSeg (+) 0 in[0..n) with Int32 offsets aux[0..m]
+ *   ACC_SK_PERMUTE  out[0..m) = histogram of the Int32 indices in[0..n) (permute (+) zeros idx 1)
+ *   ACC_SK_STENCIL  out = 5-point stencil (0.25 N/S/E/W, -1 centre, clamp) of the n x m grid in */
+typedef enum acc_skeleton {
+  ACC_SK_FOLD = 0,
+  ACC_SK_SCAN = 1,
+  ACC_SK_FOLDSEG = 2,
+  ACC_SK_PERMUTE = 3,
+  ACC_SK_STENCIL = 4
+} acc_skeleton;
+
+typedef struct acc_serve_req {
+  int skeleton;      /* acc_skeleton                                         */
+  int type;          /* element type (permute: ACC_I32)                      */
+  const void *in;
+  const void *aux;   /* foldSeg offsets, else unused                          */
+  void *out;
+  int64_t n;         /* elements (stencil: grid rows)                         */
+  int64_t m;         /* foldSeg segments / permute bins / stencil grid columns */
+  double arrival;    /* seconds after the start of the run, non-decreasing    */
+} acc_serve_req;
+
+typedef struct acc_serve_stats {
+  double wall_s;         /* from the first arrival to the last completion seen */
+  int64_t served;
+  int64_t batches;       /* batched launches (mode 0)                          */
+  int64_t max_inflight;  /* most requests on the GPU at once                   */
+  int64_t peak_bytes;    /* most bytes held by admitted requests               */
+} acc_serve_stats;
+
+/* Serve `reqs` (sorted by arrival) and write each request's latency in
+ * seconds (completion seen by the host minus arrival).  mode 0: continuous
+ * batching over `slots` streams with a device-memory admission budget of
+ * `budget_bytes` (bytes of input + output held by admitted requests);
+ * mode 1: plain per-call launches in arrival order on one stream.  The call
+ * first synchronises the device (the inputs may still be in flight on the
+ * caller's streams) and blocks until every request is served. */
+int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t budget_bytes,
+                  int slots, int mode, double *latency, acc_serve_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,29 @@ def test_batch_graph_replays(acc, dev):
     b.close()
 
 
+def test_batch_mixed_types_in_any_order(acc, dev):
+    # 8-byte requests first, then 4-byte multi-tile folds: every fold tile
+    # partial needs its own slot whatever the element size of its neighbours.
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    reqs = []
+    for rep in range(6):
+        for dt in (torch.float64, torch.int64, torch.float32, torch.int32):
+            n = 3000 + 1777 * rep
+            if dt.is_floating_point:
+                xs = torch.randn(n, dtype=dt, device=dev, generator=g)
+            else:
+                xs = torch.randint(-100, 100, (n,), dtype=dt, device=dev, generator=g)
+            reqs.append(("fold", xs, torch.zeros(1, dtype=dt, device=dev), 0))
+    b = acc.Batch("+", reqs)
+    for _ in range(2):
+        b.launch()
+        b.status()
+        for kind, xs, out, z in reqs:
+            check(out, acc.fold("+", 0, xs).reshape(1), xs, "+")
+    b.close()
+
+
 def test_batch_uses_a_loaded_tuning_table(acc, dev, tmp_path):
     entries = [[k, t, bucket, 2] for k in (0, 1) for t in (0, 1, 3, 4) for bucket in range(8, 23)]
     p = tmp_path / "tune.json"

@@ -45,11 +45,17 @@ BYTES = {
     "permute": 4 * N_PERM + 2 * 4 * M_PERM,
     "stencil": 8 * H_ST * W_ST,
 }
-# DRAM bytes per launch of the scan kernel: dram__bytes_read.sum +
-# dram__bytes_write.sum of one ncu capture at 2^25 Int64 elements
-# (268.6 MB + 212.0 MB; profiles/scan_tma_kernel_int64.md), scaled by the
-# element count to the 2^28 launch (traffic grows in proportion).
-NCU_TRAFFIC = {"scan": int((268.6e6 + 212.0e6) * 8)}
+# DRAM bytes per full-size launch of each skeleton's kernel:
+# dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the
+# `bench.py --only <skeleton> --scale <s>` small case, scaled by the units
+# processed to the full launch (traffic grows in proportion; the stencil case
+# is already full size).  Summaries with the commands sit in profiles/.
+NCU_TRAFFIC = {
+    "scan": int((268.570368e6 + 213.748992e6) * 8),   # 2^25 Int64 -> 2^28
+    "fold": int((268.478208e6 + 2.757376e6) * 4),     # 2^26 Float32 -> 2^28
+    "permute": int((268.722688e6 + 2.906368e6) * 4),  # 2^26 indices -> 2^28
+    "stencil": int(292.122624e6 + 222.595328e6),      # 8192^2, full size
+}
 
 # foldSeg workload: 2^26 Float32 values ~ N(0,1) in 2^20 segments with
 # lognormal lengths (median 48, sigma 1.5, capped at 2^16, 2 % empty),
@@ -246,7 +252,8 @@ def run_ours(args, rank, world):
     for nm in names:
         ms = statistics.mean(per[nm])
         gbs = BYTES[nm] / (ms * 1e-3) / 1e9
-        per_sk[nm] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
+        per_sk[nm] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3),
+                      "traffic": NCU_TRAFFIC[nm]}
     clocks = clk.summary()
     line = {
         "metric": "HBM GB/s per skeleton vs peak (plain single-call kernels at full size)",

@@ -65,14 +65,13 @@ __device__ __forceinline__ void b_publish(uint64_t *status, int64_t t, uint32_t 
 }
 template <class S>
 __device__ __forceinline__ uint32_t b_peek(const uint64_t *status, int64_t t, uint32_t epoch, S &v) {
-  uint64_t w0 = ld_relaxed_u64(status + 2 * t);
-  uint32_t tag = (uint32_t)(w0 >> 32);
+  const SlotWords s = ld_slot(status + 2 * t);  // both words in one access
+  const uint32_t tag = (uint32_t)(s.w0 >> 32);
   if ((tag >> 2) != epoch) return 0;
-  uint64_t b = w0 & 0xffffffffull;
+  uint64_t b = s.w0 & 0xffffffffull;
   if constexpr (sizeof(S) == 8) {
-    uint64_t w1 = ld_relaxed_u64(status + 2 * t + 1);
-    if ((uint32_t)(w1 >> 32) != tag) return 0;
-    b |= (w1 & 0xffffffffull) << 32;
+    if ((uint32_t)(s.w1 >> 32) != tag) return 0;
+    b |= (s.w1 & 0xffffffffull) << 32;
   }
   v = from_bits<S>(b);
   return tag & 3u;

@@ -284,6 +284,18 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p) {
   return v;
 }
 
+// Both 64-bit words of a look-back status slot in one 16-byte access (slots
+// are 16-byte aligned).  The pair is not read atomically; every word carries
+// its own tag, so a reader rejects a pair taken from two publications.
+// Loading a slot whole lets a poll issue all of its slot loads back to back
+// instead of paying one round trip per word.
+struct SlotWords { uint64_t w0, w1; };
+__device__ __forceinline__ SlotWords ld_slot(const uint64_t *p) {
+  SlotWords s;
+  asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(s.w0), "=l"(s.w1) : "l"(p) : "memory");
+  return s;
+}
+
 // Coherent (L1-bypassing) load of a state written by another CTA of this grid.
 template <class S> __device__ __forceinline__ S ld_state(const S *p) {
   if constexpr (sizeof(S) == 4) {

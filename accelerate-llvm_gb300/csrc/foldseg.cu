@@ -237,15 +237,13 @@ __device__ __forceinline__ void publish_seg(uint64_t *status, int64_t t, uint32_
   st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
 }
 template <class S>
-__device__ __forceinline__ uint32_t peek_seg(const uint64_t *status, int64_t t, uint32_t epoch, S &v, bool &end) {
-  uint64_t w0 = ld_relaxed_u64(status + 2 * t);
-  uint32_t tag = (uint32_t)(w0 >> 32);
+__device__ __forceinline__ uint32_t decode_seg(SlotWords s, uint32_t epoch, S &v, bool &end) {
+  const uint32_t tag = (uint32_t)(s.w0 >> 32);
   if ((tag >> 3) != epoch) return 0;
-  uint64_t b = w0 & 0xffffffffull;
+  uint64_t b = s.w0 & 0xffffffffull;
   if constexpr (sizeof(S) == 8) {
-    uint64_t w1 = ld_relaxed_u64(status + 2 * t + 1);
-    if ((uint32_t)(w1 >> 32) != tag) return 0;
-    b |= (w1 & 0xffffffffull) << 32;
+    if ((uint32_t)(s.w1 >> 32) != tag) return 0;
+    b |= (s.w1 & 0xffffffffull) << 32;
   }
   v = from_bits<S>(b);
   end = (tag >> 2) & 1u;
@@ -427,10 +425,16 @@ foldseg_scan_kernel(const __grid_constant__ CUtensorMap tin, SegScanArgs a) {
         }
         uint32_t it = 0;
         while (true) {
+          SlotWords sw[LB];
+#pragma unroll
+          for (int i = 0; i < LB; ++i) {
+            sw[i] = SlotWords{0ull, 0ull};
+            if (fl[i] == 0) sw[i] = ld_slot(a.status + 2 * (tile - 1 - (k0 + lane * LB + i)));
+          }
           bool ready = true;
 #pragma unroll
           for (int i = 0; i < LB; ++i) {
-            if (fl[i] == 0) fl[i] = peek_seg<S>(a.status, tile - 1 - (k0 + lane * LB + i), a.epoch, v[i], en[i]);
+            if (fl[i] == 0) fl[i] = decode_seg<S>(sw[i], a.epoch, v[i], en[i]);
             ready = ready && fl[i] != 0;
           }
           if (__all_sync(0xffffffffu, ready)) break;

@@ -72,17 +72,16 @@ __device__ __forceinline__ void publish(uint64_t *status, int64_t t, uint32_t ep
   st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
 }
 
-// Read the status of tile t; returns the flag (0 = not yet published).
+// Decode a status slot read by ld_slot; returns the flag (0 = not yet
+// published in this epoch, or torn between two publications).
 template <class S>
-__device__ __forceinline__ uint32_t peek(const uint64_t *status, int64_t t, uint32_t epoch, S &v) {
-  uint64_t w0 = ld_relaxed_u64(status + 2 * t);
-  uint32_t tag = (uint32_t)(w0 >> 32);
+__device__ __forceinline__ uint32_t decode(SlotWords s, uint32_t epoch, S &v) {
+  const uint32_t tag = (uint32_t)(s.w0 >> 32);
   if ((tag >> 2) != epoch) return 0;
-  uint64_t b = w0 & 0xffffffffull;
+  uint64_t b = s.w0 & 0xffffffffull;
   if constexpr (sizeof(S) == 8) {
-    uint64_t w1 = ld_relaxed_u64(status + 2 * t + 1);
-    if ((uint32_t)(w1 >> 32) != tag) return 0;
-    b |= (w1 & 0xffffffffull) << 32;
+    if ((uint32_t)(s.w1 >> 32) != tag) return 0;
+    b |= (s.w1 & 0xffffffffull) << 32;
   }
   v = from_bits<S>(b);
   return tag & 3u;
@@ -184,13 +183,21 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
         }
         uint32_t it = 0;
         while (true) {
+          // Issue every pending slot load of this poll first, then decode:
+          // one round trip per poll, not one per slot.
+          SlotWords sw[LB];
+#pragma unroll
+          for (int i = 0; i < LB; ++i) {
+            sw[i] = SlotWords{0ull, 0ull};
+            if (ex[i] && fl[i] == 0) {
+              const int64_t d = k0 + lane * LB + i;
+              sw[i] = ld_slot(a.status + 2 * (R2L ? tile + 1 + d : tile - 1 - d));
+            }
+          }
           bool ready = true;
 #pragma unroll
           for (int i = 0; i < LB; ++i) {
-            if (ex[i] && fl[i] == 0) {
-              const int64_t d = k0 + lane * LB + i;
-              fl[i] = peek<S>(a.status, R2L ? tile + 1 + d : tile - 1 - d, a.epoch, v[i]);
-            }
+            if (ex[i] && fl[i] == 0) fl[i] = decode<S>(sw[i], a.epoch, v[i]);
             ready = ready && fl[i] != 0;
           }
           if (__all_sync(0xffffffffu, ready)) break;

@@ -233,7 +233,7 @@ def run_ours(args, rank, world):
     assert int(outs["scan"][-1].item()) == int(inp["scan"].sum().item())
 
     # ---- foldSeg and batched workloads (reported beside the metric, not part of `value`)
-    extra = {"foldseg": run_foldseg(torch, acc, args, dev)}
+    extra = {"foldseg": run_foldseg(torch, acc, args, dev), "precision": run_precision(torch, acc, inp, dev)}
     if not args.no_batch:
         extra["batched"] = run_batched(torch, acc, args, dev)
     if args.serve_seconds > 0:
@@ -312,6 +312,51 @@ def run_foldseg(torch, acc, args, dev):
         res[name] = {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
     acc.sync()
     res["workload"] = "foldSeg over 2^26 values in 2^20 lognormal segments (median 48, sigma 1.5, 2% empty)"
+    return res
+
+
+def run_precision(torch, acc, inp, dev):
+    """Float32 (+) accuracy of the three accumulation modes against an FP64
+    reference on the device: fold over the 2^28 bench input, scanl1 over its
+    first 2^26 elements, foldSeg over the lognormal segmentation.  Errors are
+    relative to the FP64 result and to the sum of magnitudes (the condition of
+    the sum); for scan and foldSeg the maximum over prefixes / segments."""
+    x = inp["fold"]
+    ref = x.double().sum()
+    mag = x.double().abs().sum()
+    res = {}
+    for mode in ("compensated", "plain", "fp64"):
+        got = acc.fold("+", 0.0, x, prec=mode).double().reshape(())
+        res.setdefault("fold_2^28", {})[mode] = {
+            "rel_err": float(abs(got - ref) / abs(ref)), "err_over_sum_abs": float(abs(got - ref) / mag)}
+    xs = x[: 1 << 26]
+    ref_s = torch.cumsum(xs.double(), 0)
+    mag_s = torch.cumsum(xs.double().abs(), 0)
+    for mode in ("compensated", "plain", "fp64"):
+        got = acc.scanl1("+", xs, prec=mode).double()
+        err = (got - ref_s).abs()
+        res.setdefault("scanl1_2^26", {})[mode] = {
+            "max_err_over_prefix_sum_abs": float((err / mag_s).max()),
+            "last_rel_err": float(err[-1] / ref_s[-1].abs())}
+        del got, err
+    del ref_s, mag_s
+    off, vals, _ = make_segments(torch, dev)
+    o = off.long()
+    cs = torch.zeros(vals.numel() + 1, dtype=torch.float64, device=dev)
+    cs[1:] = torch.cumsum(vals.double(), 0)
+    ca = torch.zeros_like(cs)
+    ca[1:] = torch.cumsum(vals.double().abs(), 0)
+    ref_g = cs[o[1:]] - cs[o[:-1]]
+    mag_g = ca[o[1:]] - ca[o[:-1]]
+    nz = mag_g > 0
+    for mode in ("compensated", "plain", "fp64"):
+        got = acc.fold_seg("+", 0.0, vals, off, prec=mode).double()
+        err = (got - ref_g).abs()
+        res.setdefault("foldSeg_2^26_in_2^20", {})[mode] = {
+            "max_err_over_seg_sum_abs": float((err[nz] / mag_g[nz]).max()),
+            "max_abs_err": float(err.max())}
+    acc.sync()
+    res["reference"] = "torch float64 sum / cumsum on the device"
     return res
 
 
@@ -430,6 +475,21 @@ def serving_stream(torch, dev, count, rate, rng, pools):
     return reqs
 
 
+def request_bytes(r):
+    """Algorithmic bytes of one serving request (inputs read + outputs written)."""
+    k, xs, aux, out, n, m, t = r
+    e = xs.element_size()
+    if k == "fold":
+        return n * e + e
+    if k == "scan":
+        return 2 * n * e
+    if k == "foldseg":
+        return n * e + 4 * (m + 1) + m * e
+    if k == "permute":
+        return 4 * n + 2 * 4 * m
+    return 2 * n * m * e
+
+
 def run_serving(torch, acc, args, dev):
     """The serving stream at 20k req/s for --serve-seconds, through the
     continuous-batching loop and through plain per-call launches; then each
@@ -458,10 +518,18 @@ def run_serving(torch, acc, args, dev):
                      "batches": st["batches"], "max_inflight": st["max_inflight"]}
     cap_n = min(count, 20000)
     burst = serving_stream(torch, dev, cap_n, 0.0, np.random.default_rng(SEED + 8), pools)
+    burst_bytes = sum(request_bytes(r) for r in burst)
+    peak, _ = peaks()
+    res["capacity_burst"] = {"requests": cap_n, "bytes": burst_bytes,
+                             "roofline_ms": round(burst_bytes / (peak * 1e9) * 1e3, 2)}
     for mode in ("batching", "per_call"):
         lat, st = acc.serve(burst, budget, slots=8, mode=mode)
         res[mode]["capacity_req_s"] = round(st["served"] / st["wall_s"])
+        res[mode]["capacity_gbs"] = round(burst_bytes / st["wall_s"] / 1e9, 1)
     res["capacity_ratio"] = round(res["batching"]["capacity_req_s"] / res["per_call"]["capacity_req_s"], 2)
+    # The most any scheduler could reach on this byte mix: every request at
+    # the HBM roofline, against the per-call rate.
+    res["capacity_ratio_ceiling"] = round(cap_n / (burst_bytes / (peak * 1e9)) / res["per_call"]["capacity_req_s"], 2)
     acc.sync()
     return res
 

@@ -296,6 +296,44 @@ __device__ __forceinline__ SlotWords ld_slot(const uint64_t *p) {
   return s;
 }
 
+// Look-back window bookkeeping (warp-collective).  Lane l holds the slots at
+// distances l * LB + i (0 = nearest predecessor) with flags fl: 0 not yet
+// published, 1 a partial value, 2 a value the walk stops at (an inclusive
+// prefix, or a tile that holds a segment end).
+//
+// Nearest lane holding a stop slot (32: none): the lanes after it need no
+// more polling.
+template <int LB>
+__device__ __forceinline__ int lb_stop_lane(const uint32_t (&fl)[LB]) {
+  bool seen = false;
+#pragma unroll
+  for (int i = 0; i < LB; ++i) seen = seen || fl[i] == 2u;
+  const unsigned pm = __ballot_sync(0xffffffffu, seen);
+  return pm ? __ffs(pm) - 1 : 32;
+}
+// Whether the window can be folded: `resolved` when it holds a stop slot and
+// every slot nearer than the nearest one is published (the slots beyond it
+// are not waited for), `whole` when it holds no stop slot and every slot is
+// published.  Returns the nearest stop lane.
+template <int LB>
+__device__ __forceinline__ int lb_window(const uint32_t (&fl)[LB], bool &resolved, bool &whole) {
+  bool all_ready = true, ready_to_p = true, seen = false;
+#pragma unroll
+  for (int i = 0; i < LB; ++i) {
+    all_ready = all_ready && fl[i] != 0u;
+    if (!seen) ready_to_p = ready_to_p && fl[i] != 0u;
+    seen = seen || fl[i] == 2u;
+  }
+  const unsigned pm = __ballot_sync(0xffffffffu, seen);
+  const unsigned rm = __ballot_sync(0xffffffffu, all_ready);
+  const int kp = pm ? __ffs(pm) - 1 : 32;
+  const unsigned below = kp >= 32 ? 0xffffffffu : ((1u << kp) - 1u);
+  const bool kp_ready = __shfl_sync(0xffffffffu, ready_to_p, kp & 31);
+  resolved = pm != 0u && (rm & below) == below && kp_ready;
+  whole = pm == 0u && rm == 0xffffffffu;
+  return kp;
+}
+
 // Coherent (L1-bypassing) load of a state written by another CTA of this grid.
 template <class S> __device__ __forceinline__ S ld_state(const S *p) {
   if constexpr (sizeof(S) == 4) {
@@ -338,6 +376,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
         : "=r"(done) : "r"(addr), "r"(phase) : "memory");
     if (done) return true;
     if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+// Bounded wait on an mbarrier phase that suspends the waiting threads (each
+// try may sleep up to 2 us until the phase completes) instead of polling, so
+// that waiting warps leave the issue slots to the CTAs that have work.  Gives
+// up after 2^20 tries (tens of milliseconds at the least, about two seconds
+// at most).  Returns false if it gave up.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t phase) {
+  uint32_t addr = smem_addr(bar);
+  for (uint32_t it = 0; it < (1u << 20); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done) : "r"(addr), "r"(phase), "r"(2000u) : "memory");
+    if (done) return true;
+    if (it > 8) __nanosleep(128);  // in case a try returns early
   }
   return false;
 }

@@ -4,20 +4,25 @@
 // segment length: a warp per segment or a CTA per segment
 // (accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/PTX/Execute.hs:343-374,
 // PTX/CodeGen/FoldSeg.hs:79-458), so skewed (lognormal) lengths leave most
-// lanes idle or most CTAs waiting on a few long segments.  Here each segment
-// is dispatched by its own length, in two launches:
-//   1. seg_classify lists the segments longer than LONG_SEG (atomic append;
-//      the order of the list does not matter, each segment is reduced alone);
-//   2. foldseg_main: the first CTAs stream the listed long segments, one CTA
-//      per segment with 16-byte vector loads; every other warp owns 32
-//      consecutive segments and reduces the short ones (<= SHORT_SEG) one per
-//      lane, serially, and the medium ones with the whole warp.
+// lanes idle or most CTAs waiting on a few long segments.  Here:
+//   * a 1-D row with 16-byte aligned values goes through foldseg_tile_kernel,
+//     one launch that cuts the VALUES into equal tiles whatever the segment
+//     lengths (see "tiled single pass" below);
+//   * other shapes (rank >= 2, unaligned values) dispatch each segment by its
+//     own length, in two launches:
+//       1. seg_classify lists the segments longer than LONG_SEG (atomic
+//          append; the order of the list does not matter, each segment is
+//          reduced alone);
+//       2. foldseg_main: the first CTAs stream the listed long segments, one
+//          CTA per segment with 16-byte vector loads; every other warp owns 32
+//          consecutive segments and reduces the short ones (<= SHORT_SEG) one
+//          per lane, serially, and the medium ones with the whole warp.
 // Per segment the result is z `f` (x_u `f` ... `f` x_(v-1)), as the native
 // backend's reduceFromTo over [seg[i], seg[i+1]) (accelerate-llvm-native/src/
 // Data/Array/Accelerate/LLVM/Native/CodeGen/FoldSeg.hs:103-141).  An empty
 // segment gives z with a seed and is left unwritten without one
 // (PTX/CodeGen/FoldSeg.hs:170-178).  Offsets that decrease or run past the
-// row are skipped and raise ACC_ERR_INDEX instead of reading out of bounds.
+// row raise ACC_ERR_INDEX instead of reading out of bounds.
 #include <cstdlib>
 #include <cstring>
 
@@ -175,69 +180,96 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
   }
 }
 
-// ----------------------------------------------------------------- segmented single pass
-// Rows of 1-D values with 16-byte aligned storage take this path: the values
-// are cut into tiles of 256 rows x 128 B (TMA, 128-byte swizzle, as in the
-// scan), independent of the segment lengths, so every CTA streams the same
-// number of bytes however skewed the segmentation is.
-//   pre-pass  seg_tiles_kernel: tile_seg[k] = the segment that contains the
-//             first element of tile k; empty segments get their seed here.
-//   main      foldseg_scan_kernel: a tile's segment ENDS (off[s+1], tile-
-//             relative, 16-bit) go to shared memory; each thread folds its
-//             128-byte row, restarting after every end; rows combine with a
-//             segmented warp / CTA scan ((f1,v1).(f2,v2) = (f1|f2, f2 ? v2 :
-//             v1 `f` v2)); the value carried into the tile comes from a
-//             segmented decoupled look-back that stops at the first
-//             predecessor holding an end; a second pass over the row writes
-//             z `f` (segment) where each segment's last element lies.
-constexpr int FS_THREADS = 256;
-constexpr int FS_ROW_BYTES = 128;
-constexpr int FS_CAP = 2048;  // segment ends per tile held in shared memory
+// ----------------------------------------------------------------- tiled single pass
+// 1-D rows with 16-byte aligned values take this path.  The values are cut
+// into tiles of 256 or 512 rows x 128 B (one 2-D TMA load per 256 rows,
+// 128-byte swizzle, as in the scan; each thread owns one or two adjacent
+// rows), independent of the segment lengths, so every CTA streams the
+// same number of bytes however skewed the segmentation is.  One launch:
+//   * a pre-pass (foldseg_tile_index) records for every tile the index of
+//     the first offset at or after its start, so a tile knows its offset
+//     range [kf, ks) from two loads; the CTA copies those offsets
+//     (tile-relative) to shared memory, writing z for the empty segments on
+//     the way;
+//   * each thread walks its 256 bytes once: a segment boundary inside them
+//     closes the segment that was open, whose state the row parks in shared
+//     memory when it also saw that segment start; the value before the row's
+//     first boundary and after its last one are carried out;
+//   * a segmented CTA scan ((f1,v1).(f2,v2) = (f1|f2, f2 ? v2 : v1 `f` v2))
+//     gives every row the value carried in from earlier rows of the tile, and
+//     the tile's own carried-out value, which is final at once: the tile
+//     publishes it (flag 2 when the tile holds a boundary, 1 when it lies
+//     inside one segment) before it looks back;
+//   * the parked results are written out in one coalesced pass, except the
+//     segment that closes at the tile's first boundary, which needs the
+//     value carried in from earlier tiles: a decoupled look-back that stops
+//     at the nearest tile holding a boundary (usually the previous one).
+// An extra tile past the last value closes the segments that end at the
+// very end of the row.  Two launches: the index pre-pass and the tile pass.  Offsets that decrease or leave [0, n] raise
+// ACC_ERR_INDEX; the tile then writes nothing but still publishes.
+constexpr int FT_THREADS = 256;
+constexpr int FT_ROW_BYTES = 128;
+constexpr int FT_CAP = 512;   // tile-relative offsets (and their results) held in shared memory
+// Adjacent 128-byte rows per thread: two for one-word states (a longer walk
+// amortises the per-thread scan and bookkeeping), one for the compensated
+// Float32 pair, whose longer walk code does not pay for itself.
+template <class S> constexpr int ft_rpt() { return std::is_same<S, F2>::value ? 1 : 2; }
 
-struct SegScanArgs {
+struct SegTileArgs {
   const void *in;
   const void *off;
   void *out;
-  int64_t inner, nseg;
-  int off64;
+  int64_t n, nseg;
+  int64_t full_rows, ntiles;
   uint64_t seed;
   int has_seed;
-  int64_t full_rows, ntiles;
-  int64_t *tile_seg;
+  const uint64_t *tidx;  // per tile: epoch tag << 35 | first offset index >= the tile start
   uint64_t *status;
   uint32_t *ticket;
   uint32_t *err;
   uint32_t epoch;
 };
 
-__device__ __forceinline__ int64_t seg_off2(const SegScanArgs &a, int64_t i) {
-  return a.off64 ? static_cast<const int64_t *>(a.off)[i] : (int64_t) static_cast<const int32_t *>(a.off)[i];
-}
+constexpr int TIDX_SHIFT = 35;  // offset indices below 2^35; the epoch above
 
-template <class T>
-__global__ void seg_tiles_kernel(SegScanArgs a, int64_t tile_elems) {
-  const T z = from_bits<T>(a.seed);
-  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.nseg; s += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t u = seg_off2(a, s), v = seg_off2(a, s + 1);
-    if (u < 0 || v < u || v > a.inner) { raise_error(a.err, DEV_ERR_INDEX); continue; }
-    if (u == v) {
-      if (a.has_seed) static_cast<T *>(a.out)[s] = z;
-      continue;
+// Pre-pass: tidx[t] = the first k with off[k] >= t * te (t < ntiles), and
+// tidx[ntiles] = nseg + 1, each tagged with the call's epoch so that no
+// clearing is needed.  Thread k writes the tiles whose start lies in
+// (off[k-1], off[k]]; k = nseg + 1 stands for the tiles past the last offset.
+// Decreasing offsets leave tiles unwritten (their stale tag is caught later).
+template <class OT>
+__global__ void foldseg_tile_index(const OT *off, int64_t nseg, int64_t ntiles, int64_t te, uint64_t *tidx,
+                                   uint32_t epoch) {
+  const uint64_t tag = (uint64_t)epoch << TIDX_SHIFT;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k <= nseg + 1;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    int64_t t0, t1;  // tiles [t0, t1] get k
+    if (k == 0) t0 = 0;
+    else {
+      const int64_t lo = (int64_t)off[k - 1];
+      t0 = lo < 0 ? 0 : lo / te + 1;
     }
-    for (int64_t k = (u + tile_elems - 1) / tile_elems; k * tile_elems < v; ++k) a.tile_seg[k] = s;
+    if (k == nseg + 1) t1 = ntiles - 1;
+    else {
+      const int64_t hi = (int64_t)off[k];
+      t1 = hi < 0 ? -1 : hi / te;
+    }
+    if (t1 > ntiles - 1) t1 = ntiles - 1;
+    for (int64_t t = t0; t <= t1; ++t) tidx[t] = tag | (uint64_t)k;
+    if (k == nseg + 1) tidx[ntiles] = tag | (uint64_t)k;
   }
 }
 
-// Look-back slot of the segmented scan: tag = epoch << 3 | end-seen << 2 | flag.
+// Look-back slot of the tiled foldSeg: tag = epoch << 3 | flag.
 template <class S>
-__device__ __forceinline__ void publish_seg(uint64_t *status, int64_t t, uint32_t epoch, uint32_t flag, bool end, S v) {
+__device__ __forceinline__ void publish_seg(uint64_t *status, int64_t t, uint32_t epoch, uint32_t flag, S v) {
   uint64_t b = to_bits(v);
-  uint64_t tag = (uint64_t)((epoch << 3) | ((uint32_t)end << 2) | flag) << 32;
+  uint64_t tag = (uint64_t)((epoch << 3) | flag) << 32;
   if constexpr (sizeof(S) == 8) st_relaxed_u64(status + 2 * t + 1, tag | (b >> 32));
   st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
 }
 template <class S>
-__device__ __forceinline__ uint32_t decode_seg(SlotWords s, uint32_t epoch, S &v, bool &end) {
+__device__ __forceinline__ uint32_t decode_seg(SlotWords s, uint32_t epoch, S &v) {
   const uint32_t tag = (uint32_t)(s.w0 >> 32);
   if ((tag >> 3) != epoch) return 0;
   uint64_t b = s.w0 & 0xffffffffull;
@@ -246,198 +278,355 @@ __device__ __forceinline__ uint32_t decode_seg(SlotWords s, uint32_t epoch, S &v
     b |= (s.w1 & 0xffffffffull) << 32;
   }
   v = from_bits<S>(b);
-  end = (tag >> 2) & 1u;
   return tag & 3u;
 }
 
-template <int OP, class T, int PREC>
-__global__ void __launch_bounds__(FS_THREADS, 3)
-foldseg_scan_kernel(const __grid_constant__ CUtensorMap tin, SegScanArgs a) {
+template <int OP, class T, int PREC, class OT>
+__global__ void __launch_bounds__(FT_THREADS, (ft_rpt<typename Acc<OP, T, PREC>::S>() == 1 ? 5 : 3))
+foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
-  constexpr int ITEMS = FS_ROW_BYTES / sizeof(T);
+  constexpr int FT_RPT = ft_rpt<S>();
+  constexpr int ITEMS = FT_ROW_BYTES / sizeof(T);
   constexpr int VEC = 16 / sizeof(T);
-  constexpr int TE = FS_THREADS * ITEMS;
-  constexpr int NWARP = FS_THREADS / 32;
+  constexpr int W = FT_RPT * ITEMS;          // values per thread (FT_RPT adjacent rows)
+  constexpr int TE = FT_THREADS * W;
+  constexpr int SUB_BYTES = FT_THREADS * FT_ROW_BYTES;
+  constexpr int NWARP = FT_THREADS / 32;
+  constexpr int FAR = 1 << 30;  // beyond every tile-relative position
   extern __shared__ unsigned char smem_raw[];
   unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   __shared__ uint64_t bar;
-  __shared__ int64_t s_tile, s_lo, s_cnt, s_off0;
-  __shared__ uint16_t s_end[FS_CAP];
-  __shared__ S s_warp[NWARP];
-  __shared__ int s_wend[NWARP];
-  __shared__ S s_carry;
+  __shared__ int64_t s_tile, s_kf, s_cnt, s_lo, s_hi, s_first_id;
+  __shared__ int s_offs[FT_CAP];
+  __shared__ int s_rowh[FT_THREADS];  // per thread: first offset entry at or after its first value
+  __shared__ S s_res[FT_CAP];         // per entry: the state of the segment that ends there
+  __shared__ S s_wv[NWARP], s_first_v, s_tile_v;
+  __shared__ int s_wf[NWARP];
+  __shared__ int s_has_first, s_tile_f, s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const OT *off = static_cast<const OT *>(a.off);
+  T *out = static_cast<T *>(a.out);
   const T idT = Prim<OP, T>::id();
 
   if (tid == 0) {
     const uint32_t dyn = atomicAdd(a.ticket, 1u);
     if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
-    const int64_t tile = dyn;
-    s_tile = tile;
+    s_tile = dyn;
+    s_has_first = 0;
+    s_bad = 0;
     mbar_init(&bar, 1);
     fence_mbar_init();
-    mbar_expect_tx(&bar, FS_THREADS * FS_ROW_BYTES);
-    tma_load_2d(buf, &tin, 0, (int)(tile * FS_THREADS), &bar);
-    const int64_t b = tile * TE;
-    const int64_t off0 = seg_off2(a, 0);
-    auto first_seg = [&](int64_t k) -> int64_t {
-      if (k >= a.ntiles) return a.nseg;
-      const int64_t s = a.tile_seg[k];
-      if (s >= 0) return s;
-      return k * TE < off0 ? 0 : a.nseg;  // tile starts before the first / after the last segment
-    };
-    const int64_t lo = first_seg(tile), hi = first_seg(tile + 1);
-    s_lo = lo;
-    s_cnt = hi > lo ? hi - lo : 0;
-    s_off0 = off0 > b ? off0 - b : 0;  // elements of this tile before the first segment
+    mbar_expect_tx(&bar, FT_RPT * SUB_BYTES);
+#pragma unroll
+    for (int u = 0; u < FT_RPT; ++u)
+      tma_load_2d(buf + u * SUB_BYTES, &tin, 0, (int)(((int64_t)dyn * FT_RPT + u) * FT_THREADS), &bar);
   }
   __syncthreads();
   const int64_t tile = s_tile;
-  const int64_t b = tile * TE;
-  const int64_t lo = s_lo, cnt = s_cnt;
-  const int off0 = (int)(s_off0 < TE ? s_off0 : TE);
-  const bool in_smem_list = cnt <= FS_CAP;
-  // Segment s_lo + i ends at tile-relative position end(i) (exclusive).
-  if (in_smem_list) {
-    for (int64_t i = tid; i < cnt; i += FS_THREADS) {
-      int64_t e = seg_off2(a, lo + 1 + i) - b;
-      if (e < 1 || e > TE) { raise_error(a.err, DEV_ERR_INDEX); e = TE + 1; }
-      s_end[i] = (uint16_t)(e > TE ? 0xffff : e);
+  const int64_t tb = tile * TE;
+  const bool last_tile = tile == a.ntiles - 1;
+  if (tid < 32) {
+    // The offsets inside [tb, te) are [kf, ks); the last tile takes every
+    // remaining one (ks = nseg + 1).
+    const uint64_t tag = (uint64_t)a.epoch << TIDX_SHIFT, mask = (1ull << TIDX_SHIFT) - 1;
+    const uint64_t e0 = a.tidx[tile], e1 = a.tidx[tile + 1];
+    const int64_t vstart = (int64_t)off[0], vend = (int64_t)off[a.nseg];
+    if (lane == 0) {
+      const int64_t kf = (int64_t)(e0 & mask), ks = (int64_t)(e1 & mask);
+      s_kf = kf;
+      s_cnt = ks - kf;
+      // Tile-relative value window of the segments, clamped to the tile.
+      int64_t lo = vstart - tb, hi = vend - tb;
+      s_lo = lo < 0 ? 0 : (lo > TE ? TE : lo);
+      s_hi = hi < 0 ? 0 : (hi > TE ? TE : hi);
+      if ((e0 & ~mask) != tag || (e1 & ~mask) != tag || ks < kf || ks > a.nseg + 1 || (tile == 0 && kf != 0) ||
+          vstart < 0 || vend > a.n || vend < vstart)
+        s_bad = 1;
+      if (s_bad) s_cnt = 0;
     }
   }
   __syncthreads();
-  auto end_at = [&](int64_t i) -> int {
-    if (i >= cnt) return 1 << 30;
-    if (in_smem_list) return s_end[i];
-    const int64_t e = seg_off2(a, lo + 1 + i) - b;
-    return (e < 1 || e > TE) ? 1 << 30 : (int)e;
-  };
-  if (!mbar_wait(&bar, 0)) {
-    raise_error(a.err, DEV_ERR_TIMEOUT);
-    mbar_wait(&bar, 0);
-  }
-
-  const int r0 = tid * ITEMS;
-  const int64_t grow = tile * FS_THREADS + tid;
-  auto load_row = [&](T (&x)[ITEMS]) {
-    if (grow < a.full_rows) {
-#pragma unroll
-      for (int c = 0; c < ITEMS / VEC; ++c) {
-        uint4 v = *reinterpret_cast<const uint4 *>(buf + tid * FS_ROW_BYTES + ((c ^ (tid & 7)) << 4));
-        memcpy(&x[c * VEC], &v, 16);
+  const int64_t kf = s_kf, cnt = s_cnt > 0 ? s_cnt : 0;
+  const T z = from_bits<T>(a.seed);
+  // Tile-relative offsets to shared memory (the first FT_CAP of them), the
+  // per-thread first entries, checks, and z for the empty segments that
+  // start in this tile.  Entry i+1 is the first entry for the threads whose
+  // first value lies in (rel_i, rel_(i+1)]; entry 0 for those at or before rel_0.
+  if (cnt == 0) s_rowh[tid] = 0;
+  bool bad = false;
+  for (int64_t i = tid; i < cnt; i += FT_THREADS) {
+    const int64_t k = kf + i;
+    const int64_t o = (int64_t)off[k];
+    const int64_t rel = o - tb;
+    if (rel < 0 || (!last_tile && rel >= TE)) bad = true;
+    const int r = (int)(rel < 0 ? 0 : (rel > TE ? TE : rel));
+    if (i < FT_CAP) s_offs[i] = (int)(rel < 0 ? -1 : r);
+    int rn = FAR;  // the next entry, or past the tile
+    if (k < a.nseg) {
+      const int64_t o1 = (int64_t)off[k + 1];
+      if (o1 < o) bad = true;
+      else if (o1 == o && a.has_seed) out[k] = z;
+      if (i + 1 < cnt) {
+        const int64_t reln = o1 - tb;
+        rn = (int)(reln < 0 ? 0 : (reln > TE ? TE : reln));
       }
+    }
+    if (i == 0)
+      for (int t = 0; t <= r / W && t < FT_THREADS; ++t) s_rowh[t] = 0;
+    const int t_hi = rn >= TE ? FT_THREADS - 1 : rn / W;
+    for (int t = r / W + 1; t <= t_hi && t < FT_THREADS; ++t) s_rowh[t] = (int)(i + 1);
+  }
+  if (bad) s_bad = 1;
+  auto rel_at = [&](int64_t h) -> int {
+    if (h >= cnt) return FAR;
+    if (h < FT_CAP) return s_offs[h];
+    const int64_t rel = (int64_t)off[kf + h] - tb;
+    return (int)(rel < 0 ? -1 : (rel > TE ? TE : rel));
+  };
+  // One warp waits for the tile; the others block at the CTA barrier, which
+  // costs no issue slots (several CTAs share an SM and the walk is
+  // issue-bound).  The barrier orders every thread after the completed load.
+  if (warp == 0 && !mbar_wait_sleep(&bar, 0)) {
+    if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
+    mbar_wait_sleep(&bar, 0);
+  }
+  __syncthreads();
+  const bool ok = s_bad == 0;
+  if (!ok && tid == 0) raise_error(a.err, DEV_ERR_INDEX);
+  const int lo = (int)s_lo, hi = (int)s_hi;
+
+  // ---- the walk over this thread's FT_RPT adjacent rows
+  const int tb0 = tid * W;
+  int64_t h = s_rowh[tid];
+  if (h < 0 || h > cnt) h = cnt;  // only with malformed offsets (nothing is written then)
+  int np = rel_at(h);
+  S acc = A::id(), left = A::id();
+  bool started = false;
+  int64_t first_h = -1;
+  // A boundary only parks the closed segment's state (the results leave in
+  // one coalesced pass after the scan), so a lane that meets one holds its
+  // warp up for a few instructions.
+  auto boundary = [&](int p) {
+    if (!started) {
+      left = acc;
+      first_h = h;
+      started = true;
+    } else if (h < FT_CAP) {
+      s_res[h] = acc;
+    } else if (ok) {  // long offset lists only: write at once
+      const int64_t sid = kf + h - 1;
+      if (sid >= 0) out[sid] = A::lower(a.has_seed ? A::comb(A::lift(z), acc) : acc);
+    }
+    acc = A::id();
+    do { ++h; np = rel_at(h); } while (np == p);  // several offsets at p: empty segments
+  };
+  const bool masked = lo > tb0 || hi < tb0 + W;
+  auto load_chunk = [&](int c, T (&x)[VEC]) {
+    const int r = FT_RPT * tid + c / (ITEMS / VEC);  // row within the tile
+    const int cc = c % (ITEMS / VEC);                // 16-byte chunk within the row
+    if (tile * (FT_RPT * FT_THREADS) + r < a.full_rows) {
+      const int rr = r % FT_THREADS;
+      const uint4 v = *reinterpret_cast<const uint4 *>(buf + (r / FT_THREADS) * SUB_BYTES + rr * FT_ROW_BYTES +
+                                                       ((cc ^ (rr & 7)) << 4));
+      memcpy(x, &v, 16);
     } else {
       const T *src = static_cast<const T *>(a.in);
 #pragma unroll
-      for (int j = 0; j < ITEMS; ++j) x[j] = (b + r0 + j < a.inner) ? src[b + r0 + j] : idT;
-    }
-    if (r0 < off0) {
-#pragma unroll
-      for (int j = 0; j < ITEMS; ++j)
-        if (r0 + j < off0) x[j] = idT;  // not part of any segment
+      for (int q = 0; q < VEC; ++q) {
+        const int64_t gi = tb + tb0 + c * VEC + q;
+        x[q] = gi < a.n ? src[gi] : idT;
+      }
     }
   };
-  // First end strictly after this row's start: binary search.
-  int64_t i0;
-  {
-    int64_t l = 0, h = cnt;
-    while (l < h) {
-      const int64_t m = (l + h) >> 1;
-      if (end_at(m) <= r0) l = m + 1; else h = m;
-    }
-    i0 = l;
-  }
-
-  // Ends inside this row as a bit mask: bit j set when a segment ends right
-  // after element j (several list entries at one position are the empty
-  // segments that follow a non-empty one).
-  uint32_t emask = 0;
-  {
-    int64_t i = i0;
-    int e = end_at(i);
-    while (e <= r0 + ITEMS) {
-      emask |= 1u << (e - r0 - 1);
-      e = end_at(++i);
+  // Fast walk: when this thread's offsets are in shared memory they become
+  // a bit mask of boundary positions (bm) and the boundaries take entries
+  // h, h+1, ... in order, so a boundary costs a shared-memory store and no
+  // load; only a position that holds several offsets (empty segments
+  // follow) skips its extra entries by reading them (dm marks those).
+  static_assert(W <= 64, "one 64-bit boundary mask per thread");
+  int64_t h_end = tid + 1 < FT_THREADS ? (int64_t)s_rowh[tid + 1] : cnt;
+  if (h_end < h || h_end > cnt) h_end = cnt;
+  bool fast = !masked && ok && h_end <= FT_CAP;
+  uint64_t bm = 0, dm = 0;
+  if (fast) {
+    for (int64_t e = h; e < h_end; ++e) {
+      const int r = s_offs[e] - tb0;
+      if (r < 0 || r >= W) fast = false;
+      else if ((bm >> r) & 1u) dm |= 1ull << r;
+      else bm |= 1ull << r;
     }
   }
-
-  // ---- pass 1: row value since its last end (branch-free), and whether it holds an end
-  S acc = A::id();
-  const bool ended = emask != 0u;
-  {
-    T x[ITEMS];
-    load_row(x);
+  const bool rows_in_smem = tile * (FT_RPT * FT_THREADS) + FT_RPT * tid + FT_RPT - 1 < a.full_rows;
+  if (FT_RPT == 2 && fast && rows_in_smem) {
+    // The common case with two rows per thread: every value of this thread
+    // is in shared memory.  A row is unrolled whole, so every bit test and chunk address is a
+    // compile-time constant.
+    int hh = (int)h;
+#pragma unroll 1
+    for (int u = 0; u < FT_RPT; ++u) {
+      const int r = FT_RPT * tid + u;
+      const unsigned char *rowp = buf + (r / FT_THREADS) * SUB_BYTES + (r % FT_THREADS) * FT_ROW_BYTES;
+      const int key = r & 7;
+      const uint32_t b32 = (uint32_t)(bm >> (u * ITEMS));
+      const uint32_t d32 = (uint32_t)(dm >> (u * ITEMS));
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      acc = A::push(acc, x[j]);
-      if ((emask >> j) & 1u) acc = A::id();
+      for (int cc = 0; cc < ITEMS / VEC; ++cc) {
+        T x[VEC];
+        const uint4 v = *reinterpret_cast<const uint4 *>(rowp + ((cc ^ key) << 4));
+        memcpy(x, &v, 16);
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          const int j = cc * VEC + q;
+          if (b32 & (1u << j)) {
+            if (!started) {
+              left = acc;
+              first_h = hh;
+              started = true;
+            } else {
+              s_res[hh] = acc;
+            }
+            ++hh;
+            if (d32 & (1u << j)) {
+              const int pos = tb0 + u * ITEMS + j;
+              while (hh < h_end && s_offs[hh] == pos) ++hh;
+            }
+            acc = A::id();
+          }
+          acc = A::push(acc, x[q]);
+        }
+      }
+    }
+  } else if (fast) {
+    int hh = (int)h;
+#pragma unroll 1
+    for (int c = 0; c < W / VEC; ++c) {
+      T x[VEC];
+      load_chunk(c, x);
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) {
+        const int j = c * VEC + q;
+        if ((bm >> j) & 1u) {
+          if (!started) {
+            left = acc;
+            first_h = hh;
+            started = true;
+          } else {
+            s_res[hh] = acc;
+          }
+          ++hh;
+          if ((dm >> j) & 1u)
+            while (hh < h_end && s_offs[hh] == tb0 + j) ++hh;
+          acc = A::id();
+        }
+        acc = A::push(acc, x[q]);
+      }
+    }
+  } else {
+#pragma unroll 1
+    for (int c = 0; c < W / VEC; ++c) {
+      T x[VEC];
+      load_chunk(c, x);
+      const int p0 = tb0 + c * VEC;
+      if (masked) {
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          if (p0 + q == np) boundary(p0 + q);
+          acc = A::push(acc, (p0 + q >= lo && p0 + q < hi) ? x[q] : idT);
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) {
+          if (p0 + q == np) boundary(p0 + q);
+          acc = A::push(acc, x[q]);
+        }
+      }
     }
   }
-  // Segmented inclusive warp scan: (f1, v1) . (f2, v2) = (f1 | f2, f2 ? v2 : v1 `f` v2).
-  S incl = acc;
-  bool fin = ended;
+
+  // ---- segmented CTA scan of the rows' carried-out values
+  S iv = acc;
+  bool ifl = started;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    const S ov = shfl_up(incl, d);
-    const bool of = __shfl_up_sync(0xffffffffu, fin, d);
+    const S ov = shfl_up(iv, d);
+    const bool of = __shfl_up_sync(0xffffffffu, ifl, d);
     if (lane >= d) {
-      if (!fin) incl = A::comb(ov, incl);
-      fin = fin || of;
+      if (!ifl) iv = A::comb(ov, iv);
+      ifl = ifl || of;
     }
   }
-  S ex = shfl_up(incl, 1);
-  bool exf = __shfl_up_sync(0xffffffffu, fin, 1);
+  S ex = shfl_up(iv, 1);
+  bool exf = __shfl_up_sync(0xffffffffu, ifl, 1);
   if (lane == 0) { ex = A::id(); exf = false; }
-  if (lane == 31) { s_warp[warp] = incl; s_wend[warp] = fin; }
+  if (lane == 31) { s_wv[warp] = iv; s_wf[warp] = ifl; }
   __syncthreads();
   S wv = A::id();
   bool wf = false;
   for (int w = 0; w < warp; ++w) {
-    wv = s_wend[w] ? s_warp[w] : A::comb(wv, s_warp[w]);
-    wf = wf || s_wend[w];
+    wv = s_wf[w] ? s_wv[w] : A::comb(wv, s_wv[w]);
+    wf = wf || s_wf[w];
   }
-
-  // ---- segmented look-back (warp 0): the value of the segment open at the tile start
-  if (warp == 0) {
-    S tv = A::id();
-    bool tf = false;
-    for (int w = 0; w < NWARP; ++w) {
-      tv = s_wend[w] ? s_warp[w] : A::comb(tv, s_warp[w]);
-      tf = tf || s_wend[w];
+  const S cin = exf ? ex : A::comb(wv, ex);  // value of the segment open at the row start
+  const bool cinf = exf || wf;                // that segment started inside the tile
+  if (started) {
+    const S v = A::comb(cin, left);
+    if (cinf) {
+      if (first_h < FT_CAP) s_res[first_h] = v;
+      else if (ok) out[kf + first_h - 1] = A::lower(a.has_seed ? A::comb(A::lift(z), v) : v);
+    } else {
+      s_first_v = v;  // the tile's first boundary: needs the value from earlier tiles
+      s_first_id = kf + first_h - 1;
+      s_has_first = 1;
     }
-    S carry = A::id();
-    if (tile > 0) {
-      if (lane == 0) publish_seg<S>(a.status, tile, a.epoch, 1u, tf, tv);
+  }
+  if (tid == FT_THREADS - 1) {
+    s_tile_v = started ? acc : A::comb(cin, acc);
+    s_tile_f = started || cinf;
+  }
+  __syncthreads();
+
+  // ---- publish; the parked results leave; look back for the segment closing
+  // at the tile's first boundary (entry 0)
+  if (tid == 0) publish_seg<S>(a.status, tile, a.epoch, s_tile_f ? 2u : 1u, s_tile_v);
+  if (ok) {
+    const int64_t nres = cnt < FT_CAP ? cnt : FT_CAP;
+    for (int64_t e = 1 + tid; e < nres; e += FT_THREADS)
+      if (s_offs[e] > s_offs[e - 1]) {  // the first entry at its position closes a segment
+        const S v = s_res[e];
+        out[kf + e - 1] = A::lower(a.has_seed ? A::comb(A::lift(z), v) : v);
+      }
+  }
+  if (warp == 0) {
+    if (s_has_first && s_first_id >= 0) {
       constexpr int LB = 4;
+      S carry = A::id();
       int64_t k0 = 0;
       bool gave_up = false;
+      uint32_t it = 0;
       while (true) {
         uint32_t fl[LB];
-        bool en[LB];
         S v[LB];
 #pragma unroll
         for (int i = 0; i < LB; ++i) {
-          const int64_t pt = tile - 1 - (k0 + lane * LB + i);
-          fl[i] = pt >= 0 ? 0u : 2u;
-          en[i] = pt < 0;
+          fl[i] = tile - 1 - (k0 + lane * LB + i) >= 0 ? 0u : 2u;
           v[i] = A::id();
         }
-        uint32_t it = 0;
+        bool resolved = false, whole = false;
+        int kp = 32;
         while (true) {
+          const int kp0 = lb_stop_lane<LB>(fl);
           SlotWords sw[LB];
 #pragma unroll
           for (int i = 0; i < LB; ++i) {
             sw[i] = SlotWords{0ull, 0ull};
-            if (fl[i] == 0) sw[i] = ld_slot(a.status + 2 * (tile - 1 - (k0 + lane * LB + i)));
+            if (fl[i] == 0 && lane <= kp0) sw[i] = ld_slot(a.status + 2 * (tile - 1 - (k0 + lane * LB + i)));
           }
-          bool ready = true;
 #pragma unroll
-          for (int i = 0; i < LB; ++i) {
-            if (fl[i] == 0) fl[i] = decode_seg<S>(sw[i], a.epoch, v[i], en[i]);
-            ready = ready && fl[i] != 0;
-          }
-          if (__all_sync(0xffffffffu, ready)) break;
+          for (int i = 0; i < LB; ++i)
+            if (fl[i] == 0 && lane <= kp0) fl[i] = decode_seg<S>(sw[i], a.epoch, v[i]);
+          kp = lb_window<LB>(fl, resolved, whole);
+          if (resolved || whole) break;
           ++it;
           const bool stop = gave_up || it > SPIN_LIMIT ||
                             ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
@@ -446,115 +635,99 @@ foldseg_scan_kernel(const __grid_constant__ CUtensorMap tin, SegScanArgs a) {
             if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
 #pragma unroll
             for (int i = 0; i < LB; ++i)
-              if (fl[i] == 0) { fl[i] = 2u; en[i] = true; }
+              if (fl[i] == 0) fl[i] = 2u;
+            kp = lb_window<LB>(fl, resolved, whole);
             break;
           }
-          __nanosleep(it < 8 ? 32 : 128);
+          __nanosleep(it < 4 ? 64 : (it < 16 ? 256 : 1024));  // back off: the predecessor is usually close behind
         }
-        // Nearest-first fold, stopping at an inclusive prefix or a tile that
-        // holds a segment end (its value already starts after that end).
         bool stop_here = false;
         S lv = A::id();
 #pragma unroll
         for (int i = 0; i < LB; ++i) {
           if (!stop_here) lv = A::comb(v[i], lv);
-          stop_here = stop_here || fl[i] == 2u || en[i];
+          stop_here = stop_here || fl[i] == 2u;
         }
-        const unsigned pm = __ballot_sync(0xffffffffu, stop_here);
-        const int kp = pm ? __ffs(pm) - 1 : 32;
         if (lane > kp) lv = A::id();
         S wr = warp_reduce_rev<A>(lv);
         wr = shfl_idx(wr, 0);
         carry = A::comb(wr, carry);
-        if (pm) break;
+        if (resolved) break;
         k0 += 32 * LB;
       }
-      // Inclusive value at the tile end: what the next tile carries in.
-      if (lane == 0) publish_seg<S>(a.status, tile, a.epoch, 2u, true, tf ? tv : A::comb(carry, tv));
-    } else if (lane == 0) {
-      publish_seg<S>(a.status, tile, a.epoch, 2u, true, tv);
-    }
-    if (lane == 0) s_carry = carry;
-  }
-  __syncthreads();
-
-  // ---- pass 2: walk the row again from its carried-in value, writing segments
-  S run;
-  {
-    // value carried into this row: (tile carry) . (warps before) . (lanes before)
-    S c = s_carry;
-    c = wf ? wv : A::comb(c, wv);
-    run = exf ? ex : A::comb(c, ex);
-  }
-  {
-    T x[ITEMS];
-    load_row(x);
-    T *out = static_cast<T *>(a.out);
-    const T z = from_bits<T>(a.seed);
-    int64_t i = i0;
-#pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      run = A::push(run, x[j]);
-      if ((emask >> j) & 1u) {
-        // The first end of a run of equal ends closes a non-empty segment,
-        // except segment 0 when it is empty (a tile starting before off[0]).
-        if (a.has_seed || lo + i != 0 || seg_off2(a, 0) < seg_off2(a, 1))
-          out[lo + i] = A::lower(a.has_seed ? A::comb(A::lift(z), run) : run);
-        run = A::id();
-        const int e = r0 + j + 1;
-        do { ++i; } while (end_at(i) == e);
+      if (lane == 0 && ok) {
+        const S v = A::comb(carry, s_first_v);
+        out[s_first_id] = A::lower(a.has_seed ? A::comb(A::lift(z), v) : v);
       }
     }
   }
 }
 
-template <int OP, class T, int PREC>
-int foldseg_scan_typed(Workspace *w, const T *in, const void *off, int off64, T *out, int64_t inner,
-                       int64_t nseg, bool has_seed, uint64_t seed, cudaStream_t s, bool *taken) {
-  constexpr int ITEMS = FS_ROW_BYTES / sizeof(T);
-  constexpr int64_t TE = (int64_t)FS_THREADS * ITEMS;
-  *taken = false;
-  const int64_t full_rows = inner / ITEMS;
-  CUtensorMap tin;
-  memset(&tin, 0, sizeof(tin));
-  if (full_rows == 0 || !encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, FS_ROW_BYTES, ITEMS, FS_THREADS, true))
-    return ACC_OK;  // not describable by TMA: the caller uses the per-segment kernels
-  const int64_t ntiles = cdiv_h(inner, TE);
-  if (ntiles >= (1ll << 31)) return ACC_OK;
-  *taken = true;
-  int st = ws_status(w, (size_t)ntiles * 2);
-  if (st) return st;
-  st = ws_scratch(w, (size_t)ntiles * sizeof(int64_t) + 256);
-  if (st) return st;
-  SegScanArgs a{};
-  a.in = in; a.off = off; a.out = out;
-  a.inner = inner; a.nseg = nseg; a.off64 = off64;
-  a.seed = seed; a.has_seed = has_seed;
-  a.full_rows = full_rows; a.ntiles = ntiles;
-  a.tile_seg = static_cast<int64_t *>(w->scratch);
-  a.status = w->status;
-  a.ticket = w->words + W_TICKET;
-  a.err = w->words + W_ERR;
-  a.epoch = ws_next_epoch(w, s);
-  cudaError_t e = cudaMemsetAsync(a.tile_seg, 0xff, (size_t)ntiles * sizeof(int64_t), s);
-  if (e != cudaSuccess) return cuda_status(e);
-  const Device &d = device_info();
-  int64_t pb = cdiv_h(nseg, 256);
-  if (pb > (int64_t)d.sms * 8) pb = (int64_t)d.sms * 8;
-  if (pb < 1) pb = 1;
-  seg_tiles_kernel<T><<<(unsigned)pb, 256, 0, s>>>(a, TE);
-  st = check_launch();
-  if (st) return st;
-  const size_t smem = (size_t)FS_THREADS * FS_ROW_BYTES + 1024;
-  auto kern = foldseg_scan_kernel<OP, T, PREC>;
+// One launcher per kernel instantiation, so that each gets its own
+// shared-memory attribute (the tile needs more than the default 48 KB).
+template <int OP, class T, int PREC, class OT>
+int launch_foldseg_tile(const CUtensorMap &tin, const SegTileArgs &a, int64_t ntiles, cudaStream_t s) {
+  constexpr int FT_RPT = ft_rpt<typename Acc<OP, T, PREC>::S>();
+  const size_t smem = (size_t)FT_RPT * FT_THREADS * FT_ROW_BYTES + 1024;
+  auto kern = foldseg_tile_kernel<OP, T, PREC, OT>;
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     attr = true;
   }
-  kern<<<(unsigned)ntiles, FS_THREADS, smem, s>>>(tin, a);
+  kern<<<(unsigned)ntiles, FT_THREADS, smem, s>>>(tin, a);
   return check_launch();
+}
+
+template <int OP, class T, int PREC>
+int foldseg_tile_typed(Workspace *w, const T *in, const void *off, int off64, T *out, int64_t inner,
+                       int64_t nseg, bool has_seed, uint64_t seed, cudaStream_t s, bool *taken) {
+  constexpr int ITEMS = FT_ROW_BYTES / sizeof(T);
+  constexpr int FT_RPT = ft_rpt<typename Acc<OP, T, PREC>::S>();
+  constexpr int64_t TE = (int64_t)FT_THREADS * FT_RPT * ITEMS;
+  *taken = false;
+  const int64_t full_rows = inner / ITEMS;
+  CUtensorMap tin;
+  memset(&tin, 0, sizeof(tin));
+  if (full_rows == 0 || !encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, FT_ROW_BYTES, ITEMS, FT_THREADS, true))
+    return ACC_OK;  // not describable by TMA: the caller uses the per-segment kernels
+  // One tile more than the values need when they fill the last tile exactly:
+  // that tile holds the boundary at position n.
+  const int64_t ntiles = inner / TE + 1;
+  if (ntiles * FT_RPT * FT_THREADS >= (1ll << 31)) return ACC_OK;  // TMA row coordinates are 32-bit
+  if (nseg + 2 >= (1ll << TIDX_SHIFT)) return ACC_OK;
+  *taken = true;
+  int st = ws_status(w, (size_t)ntiles * 2);
+  if (st) return st;
+  st = ws_scratch(w, (size_t)(ntiles + 1) * sizeof(uint64_t));
+  if (st) return st;
+  SegTileArgs a{};
+  a.in = in; a.off = off; a.out = out;
+  a.n = inner; a.nseg = nseg;
+  a.full_rows = full_rows; a.ntiles = ntiles;
+  a.seed = seed; a.has_seed = has_seed;
+  a.tidx = static_cast<const uint64_t *>(w->scratch);
+  a.status = w->status;
+  a.ticket = w->words + W_TICKET;
+  a.err = w->words + W_ERR;
+  a.epoch = ws_next_epoch(w, s);
+  {
+    const Device &d = device_info();
+    int64_t pb = cdiv_h(nseg + 2, 256);
+    if (pb > (int64_t)d.sms * 8) pb = (int64_t)d.sms * 8;
+    uint64_t *tidx = static_cast<uint64_t *>(w->scratch);
+    if (off64)
+      foldseg_tile_index<int64_t><<<(unsigned)pb, 256, 0, s>>>(static_cast<const int64_t *>(off), nseg, ntiles, TE,
+                                                                tidx, a.epoch);
+    else
+      foldseg_tile_index<int32_t><<<(unsigned)pb, 256, 0, s>>>(static_cast<const int32_t *>(off), nseg, ntiles, TE,
+                                                                tidx, a.epoch);
+    st = check_launch();
+    if (st) return st;
+  }
+  return off64 ? launch_foldseg_tile<OP, T, PREC, int64_t>(tin, a, ntiles, s)
+               : launch_foldseg_tile<OP, T, PREC, int32_t>(tin, a, ntiles, s);
 }
 
 // ----------------------------------------------------------------- host side
@@ -605,12 +778,13 @@ int foldseg_dispatch(Workspace *w, int op, int type, int prec, const void *in, c
       constexpr int OP = decltype(opc)::value;
       return with_prec<OP, T>(prec, [&](auto pc) -> int {
         constexpr int P = decltype(pc)::value;
-        // The segmented single-pass kernel is opt-in (ACC_GB300_FOLDSEG=scan):
-        // on GB300 it is still slower than the per-segment kernels.
-        static const bool seg_scan = getenv("ACC_GB300_FOLDSEG") && strcmp(getenv("ACC_GB300_FOLDSEG"), "scan") == 0;
-        if (outer == 1 && seg_scan) {
+        // Rows of one segmented vector take the tiled single pass unless
+        // ACC_GB300_FOLDSEG=segments asks for the per-segment kernels.
+        static const bool per_segment =
+            getenv("ACC_GB300_FOLDSEG") && strcmp(getenv("ACC_GB300_FOLDSEG"), "segments") == 0;
+        if (outer == 1 && !per_segment) {
           bool taken = false;
-          const int st = foldseg_scan_typed<OP, T, P>(w, static_cast<const T *>(in), off, off64,
+          const int st = foldseg_tile_typed<OP, T, P>(w, static_cast<const T *>(in), off, off64,
                                                       static_cast<T *>(out), inner, nseg, seed != nullptr, sb, s,
                                                       &taken);
           if (taken || st) return st;

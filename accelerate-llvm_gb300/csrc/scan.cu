@@ -182,25 +182,27 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
           v[i] = A::id();
         }
         uint32_t it = 0;
+        bool resolved = false, whole = false;
+        int kp = 32;
         while (true) {
           // Issue every pending slot load of this poll first, then decode:
-          // one round trip per poll, not one per slot.
+          // one round trip per poll, not one per slot.  Lanes beyond the
+          // nearest inclusive prefix seen so far need no more reads.
+          const int kp0 = lb_stop_lane<LB>(fl);
           SlotWords sw[LB];
 #pragma unroll
           for (int i = 0; i < LB; ++i) {
             sw[i] = SlotWords{0ull, 0ull};
-            if (ex[i] && fl[i] == 0) {
+            if (ex[i] && fl[i] == 0 && lane <= kp0) {
               const int64_t d = k0 + lane * LB + i;
               sw[i] = ld_slot(a.status + 2 * (R2L ? tile + 1 + d : tile - 1 - d));
             }
           }
-          bool ready = true;
 #pragma unroll
-          for (int i = 0; i < LB; ++i) {
-            if (ex[i] && fl[i] == 0) fl[i] = decode<S>(sw[i], a.epoch, v[i]);
-            ready = ready && fl[i] != 0;
-          }
-          if (__all_sync(0xffffffffu, ready)) break;
+          for (int i = 0; i < LB; ++i)
+            if (ex[i] && fl[i] == 0 && lane <= kp0) fl[i] = decode<S>(sw[i], a.epoch, v[i]);
+          kp = lb_window<LB>(fl, resolved, whole);
+          if (resolved || whole) break;
           ++it;
           // Give up (warp-uniformly) after SPIN_LIMIT polls, or at once when
           // another CTA on this stream has already timed out.
@@ -212,6 +214,7 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
 #pragma unroll
             for (int i = 0; i < LB; ++i)
               if (fl[i] == 0) fl[i] = 2u;  // treat as identity: the result is flagged as failed
+            kp = lb_window<LB>(fl, resolved, whole);
             break;
           }
           __nanosleep(it < 8 ? 32 : 128);
@@ -225,13 +228,11 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
           if (!seen_p) lv = R2L ? A::comb(lv, v[i]) : A::comb(v[i], lv);
           seen_p = seen_p || fl[i] == 2u;
         }
-        const unsigned pmask = __ballot_sync(0xffffffffu, seen_p);
-        const int kp = pmask ? __ffs(pmask) - 1 : 32;
         if (lane > kp) lv = A::id();
         S wv = R2L ? warp_reduce<A>(lv) : warp_reduce_rev<A>(lv);
         wv = shfl_idx(wv, 0);
         acc = R2L ? A::comb(acc, wv) : A::comb(wv, acc);
-        if (pmask) break;
+        if (resolved) break;
         k0 += 32 * LB;
       }
       prefix = acc;

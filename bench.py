@@ -232,15 +232,16 @@ def run_ours(args, rank, world):
     assert int(outs["permute"].sum().item()) == N_PERM
     assert int(outs["scan"][-1].item()) == int(inp["scan"].sum().item())
 
+    # ---- end to end through the public API with host buffers (measured first,
+    # before the other workloads allocate host and device memory)
+    e2e = run_e2e(torch, acc, inp, zeros, args, dev)
+
     # ---- foldSeg and batched workloads (reported beside the metric, not part of `value`)
     extra = {"foldseg": run_foldseg(torch, acc, args, dev), "precision": run_precision(torch, acc, inp, dev)}
     if not args.no_batch:
         extra["batched"] = run_batched(torch, acc, args, dev)
     if args.serve_seconds > 0:
         extra["serving"] = run_serving(torch, acc, args, dev)
-
-    # ---- end to end through the public API with host buffers
-    e2e = run_e2e(torch, acc, inp, zeros, args, dev)
 
     peak, peak_kind = peaks()
     step_bytes = sum(BYTES.values())

@@ -86,3 +86,19 @@ def test_foldseg_bad_offsets_raise(acc, dev):
         acc.sync()
     assert e.value.status == 7
     acc.sync()  # the error word was cleared
+
+
+def test_per_segment_kernels_on_vectors():
+    """The per-segment kernels (selected for 1-D rows by
+    ACC_GB300_FOLDSEG=segments, read once per process) give the same results:
+    the grid, size, precision and edge-case tests again in a child process."""
+    import os
+    import pathlib
+    import subprocess
+    import sys
+    env = dict(os.environ, ACC_GB300_FOLDSEG="segments")
+    here = pathlib.Path(__file__).resolve()
+    r = subprocess.run([sys.executable, "-m", "pytest", str(here), "-q", "-m", "gpu", "-p", "no:cacheprovider",
+                        "-k", "not per_segment_kernels"], cwd=here.parent.parent, env=env,
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-2000:]

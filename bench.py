@@ -246,7 +246,7 @@ def run_ours(args, rank, world):
     peak, peak_kind = peaks()
     step_bytes = sum(BYTES.values())
     ms_per_step = total_ms / args.steps
-    value = world * step_bytes / (ms_per_step * 1e-3) / 1e9
+    value = whole_job_gbs(world, step_bytes, ms_per_step)
     scan_ms = statistics.mean(per["scan"])
     achieved = BYTES["scan"] / (scan_ms * 1e-3) / 1e9
     per_sk = {}
@@ -715,13 +715,18 @@ def run_reference(args):
 
 # ----------------------------------------------------------------- distributed
 def dist_init():
+    """One process per GPU under torchrun: NCCL with a GPU, gloo without one
+    (the replica bookkeeping is the same)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     return rank, world
 
 
@@ -732,13 +737,21 @@ def dist_barrier(world):
 
 
 def dist_max(world, v):
+    """The maximum of v over the ranks (the slowest replica sets the time)."""
     if world > 1:
         import torch
         import torch.distributed as dist
-        t = torch.tensor([v], device="cuda")
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
     return v
+
+
+def whole_job_gbs(world, step_bytes, ms_per_step):
+    """Replicas only: every rank moves step_bytes per step, so the job moves
+    world * step_bytes in the slowest rank's time."""
+    return world * step_bytes / (ms_per_step * 1e-3) / 1e9
 
 
 def main():

@@ -457,71 +457,36 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
       else bm |= 1ull << r;
     }
   }
-  const bool rows_in_smem = tile * (FT_RPT * FT_THREADS) + FT_RPT * tid + FT_RPT - 1 < a.full_rows;
-  if (FT_RPT == 2 && fast && rows_in_smem) {
-    // The common case with two rows per thread: every value of this thread
-    // is in shared memory.  A row is unrolled whole, so every bit test and chunk address is a
-    // compile-time constant.
+  if (fast) {
+    // Branch-free walk: every boundary, the row's first included, parks the
+    // closed segment's state at its entry; the first one is read back as
+    // the value carried out to the left.  Only a boundary followed by empty
+    // segments branches (to skip their entries).
     int hh = (int)h;
-#pragma unroll 1
-    for (int u = 0; u < FT_RPT; ++u) {
-      const int r = FT_RPT * tid + u;
-      const unsigned char *rowp = buf + (r / FT_THREADS) * SUB_BYTES + (r % FT_THREADS) * FT_ROW_BYTES;
-      const int key = r & 7;
-      const uint32_t b32 = (uint32_t)(bm >> (u * ITEMS));
-      const uint32_t d32 = (uint32_t)(dm >> (u * ITEMS));
-#pragma unroll
-      for (int cc = 0; cc < ITEMS / VEC; ++cc) {
-        T x[VEC];
-        const uint4 v = *reinterpret_cast<const uint4 *>(rowp + ((cc ^ key) << 4));
-        memcpy(x, &v, 16);
-#pragma unroll
-        for (int q = 0; q < VEC; ++q) {
-          const int j = cc * VEC + q;
-          if (b32 & (1u << j)) {
-            if (!started) {
-              left = acc;
-              first_h = hh;
-              started = true;
-            } else {
-              s_res[hh] = acc;
-            }
-            ++hh;
-            if (d32 & (1u << j)) {
-              const int pos = tb0 + u * ITEMS + j;
-              while (hh < h_end && s_offs[hh] == pos) ++hh;
-            }
-            acc = A::id();
-          }
-          acc = A::push(acc, x[q]);
-        }
-      }
-    }
-  } else if (fast) {
-    int hh = (int)h;
+    const int h0 = hh;
 #pragma unroll 1
     for (int c = 0; c < W / VEC; ++c) {
       T x[VEC];
       load_chunk(c, x);
+      const uint32_t cb = (uint32_t)(bm >> (c * VEC)) & ((1u << VEC) - 1u);
+      const uint32_t cd = (uint32_t)(dm >> (c * VEC)) & ((1u << VEC) - 1u);
 #pragma unroll
       for (int q = 0; q < VEC; ++q) {
-        const int j = c * VEC + q;
-        if ((bm >> j) & 1u) {
-          if (!started) {
-            left = acc;
-            first_h = hh;
-            started = true;
-          } else {
-            s_res[hh] = acc;
-          }
-          ++hh;
-          if ((dm >> j) & 1u)
-            while (hh < h_end && s_offs[hh] == tb0 + j) ++hh;
-          acc = A::id();
+        const bool bnd = (cb >> q) & 1u;
+        if (bnd) s_res[hh] = acc;
+        if (bnd && ((cd >> q) & 1u)) {
+          const int pos = tb0 + c * VEC + q;
+          do { ++hh; } while (hh < h_end && s_offs[hh] == pos);
+        } else {
+          hh += bnd ? 1 : 0;
         }
+        acc = bnd ? A::id() : acc;
         acc = A::push(acc, x[q]);
       }
     }
+    started = hh != h0;
+    first_h = h0;
+    if (started) left = s_res[h0];
   } else {
 #pragma unroll 1
     for (int c = 0; c < W / VEC; ++c) {

@@ -150,15 +150,15 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
   __syncthreads();
 }
 
-template <int OP, class T, int PREC>
+template <int OP, class T, int PREC, int IPT>
 __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uint32_t epoch, unsigned char *smem) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
   __shared__ S s_warp[BT / 32];
   __shared__ S s_prefix;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int ipt = q.ipt;
-  const int pitch = ipt + 1;  // padded row: conflict-free thread-per-row access
+  constexpr int ipt = IPT;  // compile time: the staging index math is shifts and masks
+  constexpr int pitch = ipt + 1;  // padded row: conflict-free thread-per-row access
   T *tile_s = reinterpret_cast<T *>(smem + 256);
   const int64_t tile = item - q.first_item;
   const int64_t ts = (int64_t)ipt * BT;
@@ -172,6 +172,7 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
   __syncthreads();
   T *row = tile_s + tid * pitch;
   S agg = A::lift(row[0]);
+#pragma unroll
   for (int j = 1; j < ipt; ++j) agg = A::push(agg, row[j]);
   S incl = warp_scan_incl<A>(agg);
   S up = shfl_up(incl, 1);
@@ -228,6 +229,7 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
   }
   __syncthreads();
   S run = A::comb(s_prefix, A::comb(wpre, excl_lane));
+#pragma unroll
   for (int j = 0; j < ipt; ++j) {
     run = A::push(run, row[j]);
     row[j] = A::lower(run);
@@ -241,10 +243,29 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
   __syncthreads();
 }
 
+// Scan tiles are instantiated per elements-per-thread (powers of two up to
+// the 32 KiB tile limit), picked by the tile's planned value.
+template <int OP, class T, int PREC>
+__device__ __forceinline__ void b_scan_tile_any(const BatchArgs &a, const BReq &q, int64_t item, uint32_t epoch,
+                                                unsigned char *smem) {
+  switch (q.ipt) {
+    case 1: b_scan_tile<OP, T, PREC, 1>(a, q, item, epoch, smem); break;
+    case 2: b_scan_tile<OP, T, PREC, 2>(a, q, item, epoch, smem); break;
+    case 4: b_scan_tile<OP, T, PREC, 4>(a, q, item, epoch, smem); break;
+    case 8: b_scan_tile<OP, T, PREC, 8>(a, q, item, epoch, smem); break;
+    default:
+      if constexpr (sizeof(T) == 4) {
+        if (q.ipt == 32) { b_scan_tile<OP, T, PREC, 32>(a, q, item, epoch, smem); break; }
+      }
+      b_scan_tile<OP, T, PREC, 16>(a, q, item, epoch, smem);
+      break;
+  }
+}
+
 enum { BK_FOLD = 0, BK_SCAN = 1 };
 
 template <int OP>
-__global__ void __launch_bounds__(BT) batch_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(BT, 5) batch_kernel(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int64_t s_item;
   __shared__ BReq s_req;
@@ -278,10 +299,10 @@ __global__ void __launch_bounds__(BT) batch_kernel(BatchArgs a) {
       }
     } else {
       switch (q.type) {
-        case ACC_I32: b_scan_tile<OP, int32_t, 0>(a, q, item, epoch, smem); break;
-        case ACC_I64: b_scan_tile<OP, int64_t, 0>(a, q, item, epoch, smem); break;
-        case ACC_F32: b_scan_tile<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN>(a, q, item, epoch, smem); break;
-        default: b_scan_tile<OP, double, 0>(a, q, item, epoch, smem); break;
+        case ACC_I32: b_scan_tile_any<OP, int32_t, 0>(a, q, item, epoch, smem); break;
+        case ACC_I64: b_scan_tile_any<OP, int64_t, 0>(a, q, item, epoch, smem); break;
+        case ACC_F32: b_scan_tile_any<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN>(a, q, item, epoch, smem); break;
+        default: b_scan_tile_any<OP, double, 0>(a, q, item, epoch, smem); break;
       }
     }
     __syncthreads();
@@ -300,6 +321,15 @@ static std::map<TuneKey, int> g_tune;
 
 static int type_bytes(int type) { return (type == ACC_I64 || type == ACC_F64) ? 8 : 4; }
 static int max_ipt(int type) { return B_MAX_TILE_BYTES / (BT * type_bytes(type)); }
+// Elements per thread as the kernel takes them: within [1, max_ipt], rounded
+// down to a power of two (scan tiles are instantiated for those only).
+static int norm_ipt(int ipt, int type) {
+  if (ipt < 1) ipt = 1;
+  if (ipt > max_ipt(type)) ipt = max_ipt(type);
+  int p = 1;
+  while (p * 2 <= ipt) p *= 2;
+  return p;
+}
 static int bucket_of(int64_t n) {
   int b = 0;
   while (b < 62 && (int64_t(1) << (b + 1)) <= n) ++b;
@@ -374,9 +404,7 @@ static int batch_make(int op, const acc_request *reqs, int64_t count, const int3
     if (q.type != ACC_I32 && q.type != ACC_I64 && q.type != ACC_F32 && q.type != ACC_F64) return ACC_ERR_UNSUPPORTED;
     if (q.n < 0 || (q.n > 0 && (!q.in || !q.out))) return ACC_ERR_INVALID;
     if (q.kind == ACC_REQ_FOLD && q.n == 0 && !q.has_seed) return ACC_ERR_EMPTY;
-    int ipt = ipt_override ? ipt_override[i] : tuned_ipt(q.kind, q.type, q.n);
-    if (ipt < 1) ipt = 1;
-    if (ipt > max_ipt(q.type)) ipt = max_ipt(q.type);
+    const int ipt = norm_ipt(ipt_override ? ipt_override[i] : tuned_ipt(q.kind, q.type, q.n), q.type);
     const int64_t ts = (int64_t)ipt * BT;
     int64_t nt = (q.n + ts - 1) / ts;
     if (q.kind == ACC_REQ_FOLD && nt == 0) nt = 1;  // fold z [] = z: one (empty) tile writes the seed
@@ -480,7 +508,7 @@ int arena_create(int op, int64_t cap_reqs, int64_t cap_items, BatchArena **out) 
 
 // Tiles a request will take (0 if it does not fit the batch kernel).
 int64_t arena_tiles(const acc_request &q) {
-  const int ipt = std::min(std::max(tuned_ipt(q.kind, q.type, q.n), 1), max_ipt(q.type));
+  const int ipt = norm_ipt(tuned_ipt(q.kind, q.type, q.n), q.type);
   const int64_t ts = (int64_t)ipt * BT;
   const int64_t nt = (q.n + ts - 1) / ts;
   return (q.kind == ACC_REQ_FOLD && nt == 0) ? 1 : nt;
@@ -491,7 +519,7 @@ int arena_launch(BatchArena *ar, const acc_request *reqs, int64_t count, cudaStr
   int64_t nitems = 0;
   for (int64_t i = 0; i < count; ++i) {
     const acc_request &q = reqs[i];
-    int ipt = std::min(std::max(tuned_ipt(q.kind, q.type, q.n), 1), max_ipt(q.type));
+    const int ipt = norm_ipt(tuned_ipt(q.kind, q.type, q.n), q.type);
     const int64_t ts = (int64_t)ipt * BT;
     int64_t nt = (q.n + ts - 1) / ts;
     if (q.kind == ACC_REQ_FOLD && nt == 0) nt = 1;
@@ -598,7 +626,7 @@ extern "C" int acc_batch_capture(acc_batch *batch, void *stream) {
   Batch *b = reinterpret_cast<Batch *>(batch);
   if (!b) return ACC_ERR_INVALID;
   if (b->exec || b->nitems == 0) return ACC_OK;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  (void)stream;  // captured on a private stream; replays go to the launch's stream
   cudaStream_t cap = nullptr;
   cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_status(e);
@@ -609,7 +637,6 @@ extern "C" int acc_batch_capture(acc_batch *batch, void *stream) {
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
   cudaStreamDestroy(cap);
-  (void)s;
   return cuda_status(e);
 }
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "acc_sync": ([_P], _I),
     "acc_release_workspaces": ([], _I),
     "acc_fold": ([_I, _I, _I, _P, _P, _L, _L, _P, _P], _I),
+    "acc_fold_zipwith": ([_I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_fold_seg": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_fold_seg_lengths": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_scan": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
@@ -190,6 +191,33 @@ def _fold(f, z, xs, prec, stream):
     st = lib().acc_fold(op_of(f), tc, PRECS[prec], _ptr(xs), _ptr(out), outer, inner, sp, _stream(stream))
     _check(st, "fold")
     return out
+
+
+def fold_zipwith(f, g, z, xs: torch.Tensor, ys: torch.Tensor, prec=None, stream=None) -> torch.Tensor:
+    """fold f z (zipWith g xs ys) with the zipWith fused into the fold (the
+    reference's delayed fold input, PTX/CodeGen/Fold.hs:80-97); z = None gives
+    fold1.  dotp xs ys = fold_zipwith("+", "*", 0, xs, ys)."""
+    xs, ys = _dev(xs), _dev(ys)
+    if xs.shape != ys.shape or xs.dtype != ys.dtype:
+        raise ValueError("zipWith of arrays of different shapes or types")
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1] if shape else 1
+    outer_shape = shape[:-1]
+    outer = 1
+    for d in outer_shape:
+        outer *= d
+    out = torch.empty(outer_shape, dtype=xs.dtype, device=xs.device)
+    sp, _keep = _seed_ptr(tc, z)
+    st = lib().acc_fold_zipwith(op_of(f), op_of(g), tc, PRECS[prec], _ptr(xs), _ptr(ys), _ptr(out), outer, inner,
+                                sp, _stream(stream))
+    _check(st, "fold_zipwith")
+    return out
+
+
+def dotp(xs: torch.Tensor, ys: torch.Tensor, prec=None, stream=None) -> torch.Tensor:
+    """dotp xs ys = fold (+) 0 (zipWith (*) xs ys)."""
+    return fold_zipwith("+", "*", 0, xs, ys, prec=prec, stream=stream)
 
 
 # ----------------------------------------------------------------- foldSeg

@@ -237,7 +237,8 @@ def run_ours(args, rank, world):
     e2e = run_e2e(torch, acc, inp, zeros, args, dev)
 
     # ---- foldSeg and batched workloads (reported beside the metric, not part of `value`)
-    extra = {"foldseg": run_foldseg(torch, acc, args, dev), "precision": run_precision(torch, acc, inp, dev)}
+    extra = {"foldseg": run_foldseg(torch, acc, args, dev), "dotp": run_dotp(torch, acc, inp, args, dev),
+             "precision": run_precision(torch, acc, inp, dev)}
     if not args.no_batch:
         extra["batched"] = run_batched(torch, acc, args, dev)
     if args.serve_seconds > 0:
@@ -314,6 +315,34 @@ def run_foldseg(torch, acc, args, dev):
     acc.sync()
     res["workload"] = "foldSeg over 2^26 values in 2^20 lognormal segments (median 48, sigma 1.5, 2% empty)"
     return res
+
+
+def run_dotp(torch, acc, inp, args, dev):
+    """dotp xs ys = fold (+) 0 (zipWith (*) xs ys) on Float32 2^28 with the
+    zipWith fused into the fold (compensated accumulation): 8 B/element."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 9)
+    xs = inp["fold"]
+    ys = torch.randn(xs.numel(), dtype=torch.float32, device=dev, generator=g)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(1, args.warmup)):
+        acc.dotp(xs, ys)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        acc.dotp(xs, ys)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    got = float(acc.dotp(xs, ys).item())
+    ref = float((xs.double() * ys.double()).sum().item())
+    acc.sync()
+    gbs = 8 * xs.numel() / (ms * 1e-3) / 1e9
+    peak, _ = peaks()
+    return {"ms": round(ms, 4), "gbs": round(gbs, 1), "frac": round(gbs / peak, 3),
+            "rel_err_vs_fp64": abs(got - ref) / abs(ref),
+            "workload": "dotp Float32 2^28 x 2 (fused zipWith (*) -> fold (+) 0, compensated)"}
 
 
 def run_precision(torch, acc, inp, dev):

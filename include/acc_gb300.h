@@ -144,6 +144,19 @@ int acc_release_workspaces(void);
 int acc_fold(int op, int type, int prec, const void *in, void *out,
              int64_t outer, int64_t inner, const void *seed, void *stream);
 
+/* fold f z (zipWith g xs ys) / fold1 f (zipWith g xs ys): a fold whose input
+ * is the fused producer of two arrays, e.g. dotp = fold (+) 0 (zipWith (*)).
+ * Replaces foldOp / foldAllOp on a delayed zipWith input
+ * (PTX/CodeGen/Fold.hs:80-97, mkFoldAll's MIRDelayed argument): the zipped
+ * array is never written.  xs, ys: outer*inner elements each, same layout;
+ * every zipped element is g x y rounded to `type`; the fold then follows
+ * acc_fold (seed on the left, `prec` for Float32 +, empty rows as acc_fold).
+ * op in {ADD, MIN, MAX}, zop in {ADD, MUL, MIN, MAX}, type in {I32, I64,
+ * F32, F64}; other combinations give ACC_ERR_UNSUPPORTED. */
+int acc_fold_zipwith(int op, int zop, int type, int prec, const void *xs, const void *ys,
+                     void *out, int64_t outer, int64_t inner, const void *seed,
+                     void *stream);
+
 /* ---------------------------------------------------------------- foldSeg */
 
 /* foldSeg f z / fold1Seg f over a segment-OFFSET array (length nseg+1, the

@@ -635,12 +635,8 @@ int launch_foldseg_tile(const CUtensorMap &tin, const SegTileArgs &a, int64_t nt
   constexpr int FT_RPT = ft_rpt<typename Acc<OP, T, PREC>::S>();
   const size_t smem = (size_t)FT_RPT * FT_THREADS * FT_ROW_BYTES + 1024;
   auto kern = foldseg_tile_kernel<OP, T, PREC, OT>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  smem_attrs_once(kern, (int)smem, attr_done);
   kern<<<(unsigned)ntiles, FT_THREADS, smem, s>>>(tin, a);
   return check_launch();
 }

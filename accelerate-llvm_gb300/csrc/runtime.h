@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -122,6 +123,18 @@ template <int OP, class T, class F> int with_prec(int prec, F &&f) {
 }
 
 inline int64_t cdiv_h(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// A kernel's shared-memory attributes belong to the device context it runs
+// in: set them once per device (bit d of `done` for device d).
+template <class K>
+inline void smem_attrs_once(K kern, int bytes, std::atomic<uint64_t> &done, bool max_carveout = true) {
+  const int dev = device_info().id;
+  const uint64_t bit = dev >= 0 && dev < 64 ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (max_carveout) cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  done.fetch_or(bit, std::memory_order_release);
+}
 
 // Fill n elements with one value (the seed fill of empty folds and scans,
 // the reference's `generate` of the seed, PTX/CodeGen/Generate.hs:40-61).

@@ -528,22 +528,14 @@ int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_
   if (tma) {
     const size_t smem = (size_t)SUB * SCAN_THREADS * SCAN_ROW_BYTES + 1024;
     auto kern = scan_tma_kernel<OP, T, PREC, R2L, SUB>;
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      attr = true;
-    }
+    static std::atomic<uint64_t> attr_done{0};
+    smem_attrs_once(kern, (int)smem, attr_done);
     kern<<<(unsigned)ntiles, SCAN_THREADS, smem, s>>>(tin, tout, a);
     return check_launch();
   }
   auto kern = scan_lookback_kernel<OP, T, PREC, R2L>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SCAN_SMEM);
-    cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  smem_attrs_once(kern, (int)SCAN_SMEM, attr_done);
   kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(a);
   return check_launch();
 }

@@ -433,11 +433,8 @@ int stencil_fast_launch(StencilArgs a, const StencilW<T> &W, uint32_t zlo, uint3
       return stencil_pipe_launch<T, RY, RX, PAT>(a, W, zlo, zhi, s, tin, tout);
   }
   auto kern = stencil_fast_kernel<T, RY, RX, PAT>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  static std::atomic<uint64_t> attr_done{0};
+  smem_attrs_once(kern, (int)smem, attr_done, false);
   const int64_t gx = cdiv_h(a.w, SF_TW), gy = cdiv_h(a.h, SF_TH);
   if (gy > 65535 || gx > (1ll << 31) - 1) return ACC_ERR_TOO_LARGE;
   kern<<<dim3((unsigned)gx, (unsigned)gy), ST_THREADS, smem, s>>>(tin, a, W, zlo, zhi);

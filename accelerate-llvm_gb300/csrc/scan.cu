@@ -24,7 +24,8 @@
 //
 // Rows of a rank >= 2 array are scanned by scan_rows_kernel: one CTA per row
 // with a carried prefix, as the reference's `scan` (multi-dim) kernel does
-// (PTX/CodeGen/Scan.hs:746-939).
+// (PTX/CodeGen/Scan.hs:746-939); many short rows take scan_rows_warp_kernel,
+// one warp per row.
 #include <cstdlib>
 #include <cstring>
 
@@ -552,9 +553,65 @@ int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   return launch_scan_1d_sub<OP, T, PREC, R2L, 1>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
 }
 
+// Short rows, many of them: one warp per row.  The warp walks the row in
+// chunks of 32 elements (one per lane, coalesced), scans each chunk with
+// shuffles and carries the prefix in a register; the semantics are those of
+// scan_rows_kernel (seed placement, exclusive flavours, totals).
+template <int OP, class T, int PREC, bool R2L>
+__global__ void __launch_bounds__(256) scan_rows_warp_kernel(RowScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  const int lane = threadIdx.x & 31;
+  const T idT = Prim<OP, T>::id();
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = gw; r < a.outer; r += nw) {
+    const T *src = static_cast<const T *>(a.in) + r * a.in_pitch;
+    T *dst = static_cast<T *>(a.out) + r * a.out_pitch;
+    S carry = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
+    const int64_t nch = (a.inner + 31) / 32;
+    for (int64_t ci = 0; ci < nch; ++ci) {
+      const int64_t c = R2L ? nch - 1 - ci : ci;
+      const int64_t e = c * 32 + lane;
+      const T x = e < a.inner ? src[e] : idT;
+      const S v = A::lift(x);
+      S incl, ex, tot;
+      if (!R2L) {
+        incl = warp_scan_incl<A>(v);
+        const S up = shfl_up(incl, 1);
+        ex = lane == 0 ? A::id() : up;
+        tot = shfl_idx(incl, 31);
+      } else {
+        incl = warp_scan_incl_rev<A>(v);
+        const S dn = shfl_down(incl, 1);
+        ex = lane == 31 ? A::id() : dn;
+        tot = shfl_idx(incl, 0);
+      }
+      // Everything before (L2R) / after (R2L) this element within the row.
+      const S before = R2L ? A::comb(ex, carry) : A::comb(carry, ex);
+      const T yv = a.exclusive ? A::lower(before) : A::lower(A::push(before, x));
+      if (e < a.inner) dst[e] = yv;
+      carry = R2L ? A::comb(tot, carry) : A::comb(carry, tot);
+    }
+    if (lane == 0) {
+      const T total = A::lower(carry);
+      if (a.sums) static_cast<T *>(a.sums)[r] = total;
+      if (a.total_at_end) dst[a.inner] = total;
+      if (a.seed_at_end) dst[a.inner] = from_bits<T>(a.seed);
+    }
+  }
+}
+
 template <int OP, class T, int PREC, bool R2L>
 int launch_scan_rows(const RowScanArgs &a, cudaStream_t s) {
   const Device &d = device_info();
+  if (a.inner <= 512 && a.outer >= (int64_t)d.sms * 64) {
+    // a warp per row: 8 rows per CTA
+    int64_t blocks = cdiv_h(a.outer, 8);
+    if (blocks > (int64_t)d.sms * 16) blocks = (int64_t)d.sms * 16;
+    scan_rows_warp_kernel<OP, T, PREC, R2L><<<(unsigned)blocks, 256, 0, s>>>(a);
+    return check_launch();
+  }
   int64_t blocks = a.outer;
   if (blocks > (int64_t)d.sms * 8) blocks = (int64_t)d.sms * 8;
   scan_rows_kernel<OP, T, PREC, R2L><<<(unsigned)blocks, 256, 0, s>>>(a);

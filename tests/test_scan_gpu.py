@@ -89,6 +89,14 @@ def test_scan_rows(acc, orc, dev, t, op, shape):
         run_scan(acc, orc, dev, t, op, shape, d, k)
 
 
+@pytest.mark.parametrize("t,op", [("i32", "+"), ("f32", "+"), ("i64", "max"), ("f64", "+"), ("u32", "xor")])
+@pytest.mark.parametrize("shape", [(9728, 33), (10_000, 1), (9728, 300), (9728, 512), (12_000, 2048)])
+def test_scan_many_short_rows(acc, orc, dev, t, op, shape):
+    # Many rows: up to 512 elements one warp per row, longer ones one CTA per row.
+    for d, k in FLAVOURS:
+        run_scan(acc, orc, dev, t, op, shape, d, k)
+
+
 @pytest.mark.parametrize("offset", [1, 3])
 @pytest.mark.parametrize("t,op", [("i32", "+"), ("i64", "+"), ("f32", "+")])
 def test_scan_unaligned(acc, orc, dev, t, op, offset):

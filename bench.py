@@ -11,7 +11,7 @@ seeded synthetic data of the workload's shapes and distributions, generated
 on the device; every input is larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --only scan|fold|permute|stencil|foldseg [--scale S]   (one kernel, small case)
+  python bench.py --only scan|fold|permute|stencil|foldseg|batched|dotp [--scale S]   (one kernel, small case)
 
 `--impl reference` times the CPU restatement of accelerate-llvm-native (the
 reference's own CPU backend cannot be built here) on all host cores over a
@@ -390,11 +390,10 @@ def run_precision(torch, acc, inp, dev):
     return res
 
 
-def run_batched(torch, acc, args, dev, count=10_000):
-    """10,000 independent requests, a quarter each of fold (+) and scanl1 (+)
-    on Int32 and on Float32, sizes log-uniform in [2^8, 2^22]: one persistent
-    launch replayed as a CUDA graph (tiles from the autotuner) against the
-    same requests as 10,000 per-call launches."""
+def batched_requests(torch, dev, count):
+    """`count` independent requests, a quarter each of fold (+) and scanl1 (+)
+    on Int32 and on Float32, sizes log-uniform in [2^8, 2^22]; returns the
+    requests and their algorithmic bytes (fold 4n, scan 8n)."""
     rng = np.random.default_rng(SEED + 4)
     sizes = np.exp(rng.uniform(np.log(2 ** 8), np.log(2 ** 22), size=count)).astype(np.int64)
     kinds = ["fold", "scan", "fold", "scan"] * (count // 4)
@@ -415,6 +414,14 @@ def run_batched(torch, acc, args, dev, count=10_000):
         out = torch.empty((1,) if kind == "fold" else (n,), dtype=dt, device=dev)
         reqs.append((kind, xs, out, 0 if kind == "fold" else None))
         nbytes += 4 * n if kind == "fold" else 8 * n
+    return reqs, nbytes
+
+
+def run_batched(torch, acc, args, dev, count=10_000):
+    """10,000 requests (batched_requests): one persistent launch replayed as a
+    CUDA graph (tiles from the autotuner) against the same requests as 10,000
+    per-call launches."""
+    reqs, nbytes = batched_requests(torch, dev, count)
     table = ROOT / "accelerate-llvm_gb300" / "_build" / "batch_tuning.json"
     t_tune = time.perf_counter()
     if table.exists():
@@ -577,6 +584,17 @@ def run_only(args):
     if name == "foldseg":
         off, vals, ivals = make_segments(torch, dev, N_SEG_VALUES // args.scale, N_SEGS // args.scale)
         fn, nbytes = (lambda: acc.fold_seg("+", 0.0, vals, off)), BYTES_FOLDSEG // args.scale
+    elif name == "batched":
+        # 10,000 / scale requests in one persistent launch (built-in tile sizes, no graph)
+        reqs, nbytes = batched_requests(torch, dev, 10_000 // args.scale)
+        b = acc.Batch("+", reqs)
+        fn = b.launch
+    elif name == "dotp":
+        g = torch.Generator(device=dev)
+        g.manual_seed(SEED + 9)
+        xs = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
+        ys = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
+        fn, nbytes = (lambda: acc.dotp(xs, ys)), 8 * xs.numel()
     else:
         inp = make_inputs(torch, dev, args.scale)
         zeros = torch.zeros(M_PERM, dtype=torch.int32, device=dev)
@@ -794,7 +812,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch workload")
     ap.add_argument("--serve-seconds", type=float, default=3.0,
                     help="length of the 20k req/s serving stream (0: skip serving)")
-    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg"],
+    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp"],
                     help="time one skeleton alone (small-case driver for ncu captures)")
     ap.add_argument("--scale", type=int, default=1, help="with --only: 1/scale of the full input")
     args = ap.parse_args()

@@ -794,7 +794,12 @@ extern "C" int acc_fold_seg_lengths(int op, int type, int prec, const void *in, 
   Workspace *w = workspace(s, &st);
   if (!w) return st;
   std::lock_guard<std::mutex> lk(w->mu);
-  // The offsets live at the END of the scratch area, after the long list.
+  // The offsets live at the END of the scratch area.  The front part,
+  // list_bytes, holds what the fold itself keeps in scratch: the per-segment
+  // path's long-segment list (at most inner / LONG_SEG + 1 entries) or the
+  // tiled path's tile index (inner / tile + 2 entries, tiles of >= 4096
+  // values), both within list_bytes, so neither grows (and moves) the
+  // scratch under the offsets.
   const size_t esz = length_type == ACC_I64 ? 8 : 4;
   const size_t list_bytes = (size_t)(inner / LONG_SEG + 2) * sizeof(int64_t) + 256;
   const size_t off_bytes = (size_t)(nseg + 1) * esz;

@@ -96,10 +96,17 @@ __device__ __forceinline__ uint32_t decode(SlotWords s, uint32_t epoch, S &v) {
 // and rescans it from its prefix, which keeps the register count low enough
 // for many tiles per SM to be in flight.  On return the results of the full
 // rows are in `buf`.
-template <int OP, class T, int PREC, bool R2L, int SUB>
+// `sub_done(u)` runs (in every thread) after sub-tile u has been rescanned
+// into `buf`, e.g. to start its store while the next sub-tile is rescanned.
+struct NoSubDone {
+  __device__ void operator()(int) const {}
+};
+
+template <int OP, class T, int PREC, bool R2L, int SUB, class SubDone = NoSubDone>
 __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile, const ScanArgs &a,
                                                typename Acc<OP, T, PREC>::S (*s_warp)[SCAN_THREADS / 32],
-                                               typename Acc<OP, T, PREC>::S &s_prefix, bool smem_all_rows) {
+                                               typename Acc<OP, T, PREC>::S &s_prefix, bool smem_all_rows,
+                                               SubDone sub_done = SubDone{}) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
@@ -287,6 +294,7 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
           if (e0 + c * VEC + k < a.n) dst[e0 + c * VEC + k] = y[k];
       }
     }
+    sub_done(u);
   }
 }
 
@@ -368,16 +376,18 @@ scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__
     raise_error(a.err, DEV_ERR_TIMEOUT);
     mbar_wait(&bar, 0);
   }
-  scan_tile_body<OP, T, PREC, R2L, SUB>(buf, tile, a, s_warp, s_prefix, false);
-  fence_proxy_async_smem();
-  __syncthreads();
-  if (tid == 0) {
-#pragma unroll
-    for (int u = 0; u < SUB; ++u)
+  // Each sub-tile leaves by TMA as soon as it is rescanned, while the next
+  // one is rescanned; the CTA waits only for the last store's reads.
+  auto store_sub = [&](int u) {
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
       tma_store_2d(&tout, 0, (int)((tile * SUB + u) * SCAN_THREADS), buf + u * SUB_BYTES);
-    tma_store_commit();
-    tma_store_wait_read();
-  }
+      tma_store_commit();
+    }
+  };
+  scan_tile_body<OP, T, PREC, R2L, SUB>(buf, tile, a, s_warp, s_prefix, false, store_sub);
+  if (tid == 0) tma_store_wait_read();
 }
 
 // --------------------------------------------------------------------------

@@ -36,7 +36,7 @@ namespace accgb {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ROW_BYTES = 128;  // one thread row = one 128 B swizzle line
 #ifndef SCAN_LOOKBACK
-#define SCAN_LOOKBACK 4  // predecessor statuses read per lane per look-back round trip
+#define SCAN_LOOKBACK 2  // predecessor statuses read per lane per look-back poll (window of 64)
 #endif
 
 struct ScanArgs {

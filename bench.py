@@ -619,11 +619,15 @@ def run_only(args):
 
 
 def run_e2e(torch, acc, inp, zeros, args, dev):
-    """Same step through the public API with host buffers: every step copies
-    each input from pinned host memory, runs the four skeletons and copies
-    every result back.  Copies in, kernels and copies out run on three streams
-    ordered by events, skeleton by skeleton (scan first, so that its 2 GiB
-    result drains while the other inputs upload)."""
+    """Same step end to end through the C ABI with host buffers: every step
+    copies each input from pinned host memory, runs the four skeletons
+    (acc_scan, acc_fold, acc_permute_clone, acc_stencil2d on device buffers
+    allocated once) and copies every result back.  Copies in, kernels and
+    copies out run on three streams ordered by events, skeleton by skeleton
+    (scan first, so that its 2 GiB result drains while the other inputs
+    upload)."""
+    import ctypes
+    lib = acc.lib()
     host = {k: v.cpu().pin_memory() for k, v in inp.items()}
     order = [("scan", "scan"), ("fold", "fold"), ("permute", "idx"), ("stencil", "grid")]
     h2d = sum(v.numel() * v.element_size() for v in host.values())
@@ -635,37 +639,65 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
     }
     d2h = sum(v.numel() * v.element_size() for v in res_host.values())
     dev_in = {k: torch.empty_like(v, device=dev) for k, v in host.items()}
+    dev_out = {k: torch.empty_like(v, device=dev) for k, v in res_host.items()}
     s_in, s_run, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    sp = {k: ctypes.c_void_p(st.cuda_stream) for k, st in (("in", s_in), ("run", s_run), ("out", s_out))}
+    zero_f = ctypes.c_float(0.0)
+    one_i = ctypes.c_int32(1)
+    w9 = (ctypes.c_float * 9)(*[v for r in W9 for v in r])
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def run_skeleton(name):
+        if name == "scan":
+            st = lib.acc_scan(acc.ADD, acc.I64, 0, 0, 0, ptr(dev_in["scan"]), ptr(dev_out["scan"]), None,
+                              1, N_SCAN, None, sp["run"])
+        elif name == "fold":
+            st = lib.acc_fold(acc.ADD, acc.F32, 0, ptr(dev_in["fold"]), ptr(dev_out["fold"]), 1, N_FOLD,
+                              ctypes.cast(ctypes.pointer(zero_f), ctypes.c_void_p), sp["run"])
+        elif name == "permute":
+            st = lib.acc_permute_clone(acc.ADD, acc.I32, ptr(zeros), None,
+                                       ctypes.cast(ctypes.pointer(one_i), ctypes.c_void_p), ptr(dev_in["idx"]),
+                                       acc.I32, ptr(dev_out["permute"]), N_PERM, M_PERM, sp["run"])
+        else:
+            st = lib.acc_stencil2d(acc.F32, 1, 1, ctypes.cast(w9, ctypes.c_void_p), acc.CLAMP, None,
+                                   ptr(dev_in["grid"]), ptr(dev_out["stencil"]), H_ST, W_ST, sp["run"])
+        if st != 0:
+            raise acc.AccError(st, name)
 
     def step():
         for name, key in order:
+            ready = torch.cuda.Event()
             with torch.cuda.stream(s_in):
                 dev_in[key].copy_(host[key], non_blocking=True)
-                ready = torch.cuda.Event()
                 ready.record(s_in)
             s_run.wait_event(ready)
-            with torch.cuda.stream(s_run):
-                if name == "scan":
-                    out = acc.scanl1("+", dev_in["scan"], stream=s_run)
-                elif name == "fold":
-                    out = acc.fold("+", 0.0, dev_in["fold"], stream=s_run)
-                elif name == "permute":
-                    out = acc.permute("+", zeros, dev_in["idx"], 1, stream=s_run)
-                else:
-                    out = acc.stencil(W9, dev_in["grid"], "clamp", stream=s_run)
-                done = torch.cuda.Event()
-                done.record(s_run)
-                # the input buffer is reused next step only after this kernel
-                dev_in[key].record_stream(s_run)
+            run_skeleton(name)
+            done = torch.cuda.Event()
+            done.record(s_run)
             s_out.wait_event(done)
             with torch.cuda.stream(s_out):
-                res_host[name].copy_(out, non_blocking=True)
-                out.record_stream(s_out)
-            s_in.wait_event(done)  # next step's upload of this input waits for its consumer
+                res_host[name].copy_(dev_out[name], non_blocking=True)
+                drained = torch.cuda.Event()
+                drained.record(s_out)
+            s_in.wait_event(done)      # next step's upload of this input waits for its consumer
+            s_run.wait_event(drained)  # next step's kernel rewrites the output only after its copy-out
 
     for _ in range(max(1, args.warmup // 2)):
         step()
     torch.cuda.synchronize()
+    # This machine's host link, with the same pinned buffers: the e2e step can be
+    # no faster than its H2D bytes at the H2D rate (the D2H overlaps).
+    def link_gbs(dst, src, stream):
+        with torch.cuda.stream(stream):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(3):
+                dst.copy_(src, non_blocking=True)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return 3 * src.numel() * src.element_size() / (a.elapsed_time(b) * 1e-3) / 1e9
+    h2d_gbs = link_gbs(dev_in["scan"], host["scan"], s_in)
+    d2h_gbs = link_gbs(res_host["scan"], dev_in["scan"], s_out)
     steps = max(2, args.steps // 2)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -680,10 +712,17 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
     torch.cuda.synchronize()
     acc.sync(s_run)
     ms = t0.elapsed_time(t1) / steps
-    del dev_in
+    # the results that came back are the step's
+    assert int(res_host["scan"][-1]) == int(inp["scan"].sum().item())
+    assert int(res_host["permute"].sum()) == N_PERM
+    del dev_in, dev_out
+    link_ms = max(h2d / (h2d_gbs * 1e9), d2h / (d2h_gbs * 1e9)) * 1e3
     return {"value": round(sum(BYTES.values()) / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "ms_per_step": round(ms, 3),
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "path": "C ABI through the Python host layer; pinned host buffers; H2D / kernels / D2H on three streams"}
+            "link": {"h2d_gbs": round(h2d_gbs, 1), "d2h_gbs": round(d2h_gbs, 1), "bound_ms_per_step": round(link_ms, 2),
+                     "frac_of_link_bound": round(link_ms / ms, 3)},
+            "path": "C ABI entry points (ctypes) on device buffers allocated once; pinned host buffers; "
+                    "H2D / kernels / D2H on three streams"}
 
 
 # ----------------------------------------------------------------- CPU arm

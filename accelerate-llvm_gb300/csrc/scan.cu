@@ -36,7 +36,7 @@ namespace accgb {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ROW_BYTES = 128;  // one thread row = one 128 B swizzle line
 #ifndef SCAN_LOOKBACK
-#define SCAN_LOOKBACK 2  // predecessor statuses read per lane per look-back poll (window of 64)
+#define SCAN_LOOKBACK 1  // predecessor statuses read per lane per look-back poll (window of 32)
 #endif
 
 struct ScanArgs {

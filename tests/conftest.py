@@ -11,7 +11,7 @@ if str(ROOT) not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    config.addinivalue_line("markers", "slow: full-size (BASELINE-sized) cases")
+    config.addinivalue_line("markers", "slow: full-size cases (2^28 elements and up)")
 
 
 @pytest.fixture(scope="session")

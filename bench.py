@@ -697,16 +697,22 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
         step()
     torch.cuda.synchronize()
     # This machine's host link, with the same pinned buffers: the e2e step can be
-    # no faster than its H2D bytes at the H2D rate (the D2H overlaps).
-    def link_gbs(dst, src, stream):
+    # no faster than its H2D bytes at the H2D rate (the D2H overlaps).  The
+    # host link's rate varies from moment to moment, so the bound takes the
+    # best of several trials after a warm copy.
+    def link_gbs(dst, src, stream, trials=5):
+        best = 0.0
         with torch.cuda.stream(stream):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            for _ in range(3):
-                dst.copy_(src, non_blocking=True)
-            b.record(stream)
-        torch.cuda.synchronize()
-        return 3 * src.numel() * src.element_size() / (a.elapsed_time(b) * 1e-3) / 1e9
+            dst.copy_(src, non_blocking=True)
+            for _ in range(trials):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(2):
+                    dst.copy_(src, non_blocking=True)
+                b.record(stream)
+                torch.cuda.synchronize()
+                best = max(best, 2 * src.numel() * src.element_size() / (a.elapsed_time(b) * 1e-3) / 1e9)
+        return best
     h2d_gbs = link_gbs(dev_in["scan"], host["scan"], s_in)
     d2h_gbs = link_gbs(res_host["scan"], dev_in["scan"], s_out)
     steps = max(2, args.steps // 2)

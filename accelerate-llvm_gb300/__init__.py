@@ -80,6 +80,7 @@ SIGNATURES = {
     "acc_fold_seg_lengths": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_scan": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_scan_noalloc": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
+    "acc_scan_zipwith": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_permute": ([_I, _I, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_permute_clone": ([_I, _I, _P, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_stencil2d": ([_I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _P], _I),
@@ -293,6 +294,36 @@ def scanl_(f, z, xs, prec=None, stream=None):
 
 def scanr_(f, z, xs, prec=None, stream=None):
     return _scan(f, z, xs, R2L, SCAN_PRIME, prec, stream)
+
+
+_SCAN_FLAVOURS = {"scanl": (L2R, SCAN_SEEDED), "scanl1": (L2R, SCAN_INCLUSIVE), "scanr": (R2L, SCAN_SEEDED),
+                  "scanr1": (R2L, SCAN_INCLUSIVE), "scanl_": (L2R, SCAN_PRIME), "scanr_": (R2L, SCAN_PRIME)}
+
+
+def scan_zipwith(flavour, f, g, z, xs: torch.Tensor, ys: torch.Tensor, prec=None, stream=None):
+    """A scan of the fused producer zipWith g xs ys, e.g.
+    scan_zipwith("scanl1", "+", "*", None, xs, ys) = scanl1 (+) (zipWith (*) xs ys).
+    `flavour` names the scan as the functions above do (scanl, scanl1, scanr,
+    scanr1, scanl_, scanr_); z is ignored by scanl1 / scanr1.  The zipped array
+    is never written (acc_scan_zipwith)."""
+    direction, kind = _SCAN_FLAVOURS[flavour]
+    xs, ys = _dev(xs), _dev(ys)
+    if xs.shape != ys.shape or xs.dtype != ys.dtype:
+        raise ValueError("zipWith of arrays of different shapes or types")
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1]
+    outer = 1
+    for d in shape[:-1]:
+        outer *= d
+    out_inner = inner + 1 if kind == SCAN_SEEDED else inner
+    out = torch.empty(shape[:-1] + (out_inner,), dtype=xs.dtype, device=xs.device)
+    sums = torch.empty(shape[:-1], dtype=xs.dtype, device=xs.device) if kind == SCAN_PRIME else None
+    sp, _keep = _seed_ptr(tc, None if kind == SCAN_INCLUSIVE else z)
+    st = lib().acc_scan_zipwith(op_of(f), op_of(g), tc, PRECS[prec], direction, kind, _ptr(xs), _ptr(ys), _ptr(out),
+                                _ptr(sums) if sums is not None else None, outer, inner, sp, _stream(stream))
+    _check(st, "scan_zipwith")
+    return (out, sums) if kind == SCAN_PRIME else out
 
 
 # ----------------------------------------------------------------- permute

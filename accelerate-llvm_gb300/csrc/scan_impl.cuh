@@ -1,0 +1,840 @@
+// scan_impl.cuh -- the scan kernels and their launchers, shared by scan.cu
+// (acc_scan, acc_scan_noalloc) and scan_zip.cu (scans over a fused
+// zipWith producer).
+//
+// scanl / scanl1 / scanr / scanr1 / scanl' / scanr' for the fixed
+// primitives.
+//
+// The reference runs a 1-D scan as three kernels (scanP1 block scans, a
+// single-block scanP2 over the block totals, scanP3 adding the carries:
+// accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/PTX/Execute.hs:422-468,
+// PTX/CodeGen/Scan.hs:141-439), about 4n words of traffic.  Here a 1-D scan is
+// ONE pass of 2n words: a single-pass scan with decoupled look-back
+// (Merrill & Garland 2016).  Each CTA
+//   1. takes a tile index from an atomic ticket (tiles are handed out in
+//      order, so every tile it may wait on belongs to a CTA that is running),
+//   2. pulls its 32 KiB tile into shared memory with one 2-D TMA load of a
+//      [rows x 128 B] view of the array, 128-byte swizzled so that the
+//      thread-per-row reads below are bank-conflict free,
+//   3. reduces each thread's 128-byte row serially, scans the thread totals
+//      with warp shuffles, publishes the tile aggregate, and (warp 0) looks
+//      back over the predecessors' published aggregates / inclusive prefixes,
+//   4. rescans its row from the tile prefix and writes the result back to the
+//      same swizzled smem buffer, from which one TMA store writes the tile.
+// Element semantics follow accelerate-llvm-native/src/Data/Array/Accelerate/
+// LLVM/Native/CodeGen/Scan.hs:136-270: left-to-right combines `f acc x`,
+// right-to-left `f x acc`; the seed sits at the far left (L2R) or far right
+// (R2L).  The primitives are commutative, so one push() serves both.
+//
+// Rows of a rank >= 2 array are scanned by scan_rows_kernel: one CTA per row
+// with a carried prefix, as the reference's `scan` (multi-dim) kernel does
+// (PTX/CodeGen/Scan.hs:746-939); many short rows take scan_rows_warp_kernel,
+// one warp per row.
+#pragma once
+
+#include <cstdlib>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace accgb {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ROW_BYTES = 128;  // one thread row = one 128 B swizzle line
+#ifndef SCAN_LOOKBACK
+#define SCAN_LOOKBACK 1  // predecessor statuses read per lane per look-back poll (window of 32)
+#endif
+
+struct ScanArgs {
+  const void *in;
+  void *out;
+  void *total_out;   // grand total (scanl z -> out+n, scan' -> sums) or null
+  void *seed_out;    // where to store the seed (scanr z -> out+n) or null
+  int64_t n;
+  int64_t full_rows;  // rows of 128 B fully inside the array
+  int64_t ntiles;
+  uint64_t seed;      // seed bits
+  uint64_t *status;
+  uint32_t *ticket;
+  uint32_t *err;
+  uint32_t epoch;
+  int has_seed;
+  int exclusive;
+  int tma_in;
+  int tma_out;
+  const void *in2;   // ZIP kernels: the scanned element i is zop(in[i], in2[i])
+  int zop;
+};
+
+// One element of a fused zipWith producer: g x y for the primitive g, in the
+// element type (integers wrap; __fmul_rn / __fadd_rn keep each product or
+// sum rounded on its own, never contracted into the scan's accumulation).
+template <class T>
+__device__ __forceinline__ T zip_elem(int zop, T x, T y) {
+  switch (zop) {
+    case ACC_ADD: return Prim<ACC_ADD, T>::ap(x, y);
+    case ACC_MUL: return Prim<ACC_MUL, T>::ap(x, y);
+    case ACC_MIN: return Prim<ACC_MIN, T>::ap(x, y);
+    default: return Prim<ACC_MAX, T>::ap(x, y);
+  }
+}
+
+__device__ __forceinline__ int swz(int row, int chunk) { return row * SCAN_ROW_BYTES + ((chunk ^ (row & 7)) << 4); }
+
+// Publish a look-back status of tile t: (flag, value), flag 1 = aggregate,
+// 2 = inclusive prefix.  Each 64-bit slot word carries the 32-bit tag
+// (epoch << 2 | flag) next to 32 bits of the value, so every word is
+// self-describing; an 8-byte value uses two words that a reader accepts only
+// when both carry the same tag.
+template <class S>
+__device__ __forceinline__ void publish(uint64_t *status, int64_t t, uint32_t epoch, uint32_t flag, S v) {
+  uint64_t b = to_bits(v);
+  uint64_t tag = (uint64_t)((epoch << 2) | flag) << 32;
+  if constexpr (sizeof(S) == 8) st_relaxed_u64(status + 2 * t + 1, tag | (b >> 32));
+  st_relaxed_u64(status + 2 * t, tag | (b & 0xffffffffull));
+}
+
+// Decode a status slot read by ld_slot; returns the flag (0 = not yet
+// published in this epoch, or torn between two publications).
+template <class S>
+__device__ __forceinline__ uint32_t decode(SlotWords s, uint32_t epoch, S &v) {
+  const uint32_t tag = (uint32_t)(s.w0 >> 32);
+  if ((tag >> 2) != epoch) return 0;
+  uint64_t b = s.w0 & 0xffffffffull;
+  if constexpr (sizeof(S) == 8) {
+    if ((uint32_t)(s.w1 >> 32) != tag) return 0;
+    b |= (s.w1 & 0xffffffffull) << 32;
+  }
+  v = from_bits<S>(b);
+  return tag & 3u;
+}
+
+// One tile = SUB sub-tiles of 256 rows x 128 B; thread t owns row t of every
+// sub-tile.  The rows of the array's full 128 B lines are in `buf` (each
+// sub-tile 32 KiB, 128-byte swizzled); the last, partial line is read from
+// and written to global memory directly.  The row is NOT kept in registers
+// across the look-back: pass 1 folds it, pass 2 re-reads it from shared memory
+// and rescans it from its prefix, which keeps the register count low enough
+// for many tiles per SM to be in flight.  On return the results of the full
+// rows are in `buf`.
+// `sub_done(u)` runs (in every thread) after sub-tile u has been rescanned
+// into `buf`, e.g. to start its store while the next sub-tile is rescanned.
+struct NoSubDone {
+  __device__ void operator()(int) const {}
+};
+
+// With ZIP, the rows read from global memory are zipped as they are read
+// (the rows in `buf` arrive zipped).
+template <int OP, class T, int PREC, bool R2L, int SUB, bool ZIP = false, class SubDone = NoSubDone>
+__device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile, const ScanArgs &a,
+                                               typename Acc<OP, T, PREC>::S (*s_warp)[SCAN_THREADS / 32],
+                                               typename Acc<OP, T, PREC>::S &s_prefix, bool smem_all_rows,
+                                               SubDone sub_done = SubDone{}) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int NWARP = SCAN_THREADS / 32;
+  constexpr int SUB_BYTES = SCAN_THREADS * SCAN_ROW_BYTES;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T idT = Prim<OP, T>::id();
+  const int64_t row0 = tile * (int64_t)(SUB * SCAN_THREADS);
+
+  auto load_row = [&](int u, T (&x)[ITEMS]) {
+    const int64_t grow = row0 + u * SCAN_THREADS + tid;
+    if (smem_all_rows || grow < a.full_rows) {
+#pragma unroll
+      for (int c = 0; c < ITEMS / VEC; ++c) {
+        uint4 v = *reinterpret_cast<const uint4 *>(buf + u * SUB_BYTES + swz(tid, c));
+        memcpy(&x[c * VEC], &v, 16);
+      }
+    } else {
+      const T *src = static_cast<const T *>(a.in);
+      const int64_t e0 = grow * ITEMS;
+      if constexpr (ZIP) {
+        const T *src2 = static_cast<const T *>(a.in2);
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? zip_elem(a.zop, src[e0 + j], src2[e0 + j]) : idT;
+      } else {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
+      }
+    }
+  };
+
+  // ---- pass 1: row totals, warp scans, warp totals
+  S excl_lane[SUB];
+#pragma unroll
+  for (int u = 0; u < SUB; ++u) {
+    T x[ITEMS];
+    load_row(u, x);
+    S agg;
+    if (!R2L) {
+      agg = A::lift(x[0]);
+#pragma unroll
+      for (int j = 1; j < ITEMS; ++j) agg = A::push(agg, x[j]);
+      S incl = warp_scan_incl<A>(agg);
+      S up = shfl_up(incl, 1);
+      excl_lane[u] = lane == 0 ? A::id() : up;
+      if (lane == 31) s_warp[u][warp] = incl;
+    } else {
+      agg = A::lift(x[ITEMS - 1]);
+#pragma unroll
+      for (int j = ITEMS - 2; j >= 0; --j) agg = A::push(agg, x[j]);
+      S incl = warp_scan_incl_rev<A>(agg);
+      S dn = shfl_down(incl, 1);
+      excl_lane[u] = lane == 31 ? A::id() : dn;
+      if (lane == 0) s_warp[u][warp] = incl;
+    }
+  }
+  __syncthreads();
+
+  // ---- decoupled look-back (warp 0)
+  if (warp == 0) {
+    S bagg = s_warp[0][0];
+#pragma unroll
+    for (int k = 1; k < SUB * NWARP; ++k) bagg = A::comb(bagg, s_warp[k / NWARP][k % NWARP]);
+    const bool first = R2L ? (tile == a.ntiles - 1) : (tile == 0);
+    S prefix;
+    if (first) {
+      prefix = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
+    } else {
+      if (lane == 0) publish<S>(a.status, tile, a.epoch, 1u, bagg);
+      // Each lane inspects LB consecutive predecessors per round trip, so one
+      // window covers 32 * LB tiles.
+      constexpr int LB = SCAN_LOOKBACK;
+      S acc = A::id();
+      int64_t k0 = 0;
+      bool gave_up = false;
+      while (true) {
+        uint32_t fl[LB];
+        S v[LB];
+        bool ex[LB];
+#pragma unroll
+        for (int i = 0; i < LB; ++i) {
+          const int64_t d = k0 + lane * LB + i;  // 0 = nearest predecessor
+          const int64_t pt = R2L ? tile + 1 + d : tile - 1 - d;
+          ex[i] = R2L ? (pt < a.ntiles) : (pt >= 0);
+          fl[i] = ex[i] ? 0u : 2u;
+          v[i] = A::id();
+        }
+        uint32_t it = 0;
+        bool resolved = false, whole = false;
+        int kp = 32;
+        while (true) {
+          // Issue every pending slot load of this poll first, then decode:
+          // one round trip per poll, not one per slot.  Lanes beyond the
+          // nearest inclusive prefix seen so far need no more reads.
+          const int kp0 = lb_stop_lane<LB>(fl);
+          SlotWords sw[LB];
+#pragma unroll
+          for (int i = 0; i < LB; ++i) {
+            sw[i] = SlotWords{0ull, 0ull};
+            if (ex[i] && fl[i] == 0 && lane <= kp0) {
+              const int64_t d = k0 + lane * LB + i;
+              sw[i] = ld_slot(a.status + 2 * (R2L ? tile + 1 + d : tile - 1 - d));
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < LB; ++i)
+            if (ex[i] && fl[i] == 0 && lane <= kp0) fl[i] = decode<S>(sw[i], a.epoch, v[i]);
+          kp = lb_window<LB>(fl, resolved, whole);
+          if (resolved || whole) break;
+          ++it;
+          // Give up (warp-uniformly) after SPIN_LIMIT polls, or at once when
+          // another CTA on this stream has already timed out.
+          const bool stop = gave_up || it > SPIN_LIMIT ||
+                            ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
+          if (__any_sync(0xffffffffu, stop)) {
+            gave_up = true;
+            if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
+#pragma unroll
+            for (int i = 0; i < LB; ++i)
+              if (fl[i] == 0) fl[i] = 2u;  // treat as identity: the result is flagged as failed
+            kp = lb_window<LB>(fl, resolved, whole);
+            break;
+          }
+          __nanosleep(it < 8 ? 32 : 128);
+        }
+        // Lane-local fold from the nearest predecessor outwards, up to and
+        // including the first inclusive prefix.
+        bool seen_p = false;
+        S lv = A::id();
+#pragma unroll
+        for (int i = 0; i < LB; ++i) {
+          if (!seen_p) lv = R2L ? A::comb(lv, v[i]) : A::comb(v[i], lv);
+          seen_p = seen_p || fl[i] == 2u;
+        }
+        if (lane > kp) lv = A::id();
+        S wv = R2L ? warp_reduce<A>(lv) : warp_reduce_rev<A>(lv);
+        wv = shfl_idx(wv, 0);
+        acc = R2L ? A::comb(acc, wv) : A::comb(wv, acc);
+        if (resolved) break;
+        k0 += 32 * LB;
+      }
+      prefix = acc;
+    }
+    const S inclusive = R2L ? A::comb(bagg, prefix) : A::comb(prefix, bagg);
+    if (lane == 0) {
+      publish<S>(a.status, tile, a.epoch, 2u, inclusive);
+      s_prefix = prefix;
+      const bool last = R2L ? (tile == 0) : (tile == a.ntiles - 1);
+      if (last && a.total_out) *static_cast<T *>(a.total_out) = A::lower(inclusive);
+      if (first && a.seed_out) *static_cast<T *>(a.seed_out) = from_bits<T>(a.seed);
+    }
+  }
+  __syncthreads();
+
+  // ---- pass 2: rescan each row from its prefix, results back to buf / global
+  T *dst = static_cast<T *>(a.out);
+#pragma unroll
+  for (int u = 0; u < SUB; ++u) {
+    // Everything before (L2R) / after (R2L) this thread's row within the tile.
+    S inner = A::id();
+    if (!R2L) {
+      for (int k = 0; k < u * NWARP + warp; ++k) inner = A::comb(inner, s_warp[k / NWARP][k % NWARP]);
+    } else {
+      for (int k = u * NWARP + warp + 1; k < SUB * NWARP; ++k) inner = A::comb(inner, s_warp[k / NWARP][k % NWARP]);
+    }
+    S run = R2L ? A::comb(A::comb(excl_lane[u], inner), s_prefix) : A::comb(s_prefix, A::comb(inner, excl_lane[u]));
+    T x[ITEMS];
+    load_row(u, x);
+    const int64_t grow = row0 + u * SCAN_THREADS + tid;
+    const bool in_smem = smem_all_rows || grow < a.full_rows;
+    const int64_t e0 = grow * ITEMS;
+#pragma unroll
+    for (int cc = 0; cc < ITEMS / VEC; ++cc) {
+      const int c = R2L ? ITEMS / VEC - 1 - cc : cc;
+      T y[VEC];
+#pragma unroll
+      for (int kk = 0; kk < VEC; ++kk) {
+        const int k = R2L ? VEC - 1 - kk : kk;
+        const int j = c * VEC + k;
+        if (a.exclusive) { y[k] = A::lower(run); run = A::push(run, x[j]); }
+        else { run = A::push(run, x[j]); y[k] = A::lower(run); }
+      }
+      if (in_smem) {
+        uint4 v;
+        memcpy(&v, y, 16);
+        *reinterpret_cast<uint4 *>(buf + u * SUB_BYTES + swz(tid, c)) = v;
+      } else {
+#pragma unroll
+        for (int k = 0; k < VEC; ++k)
+          if (e0 + c * VEC + k < a.n) dst[e0 + c * VEC + k] = y[k];
+      }
+    }
+    sub_done(u);
+  }
+}
+
+// One tile per CTA, any alignment: coalesced loads / stores through the same
+// swizzled smem layout (used when a TMA descriptor cannot describe the array).
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(ScanArgs a) {
+  using S = typename Acc<OP, T, PREC>::S;
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int TILE = SCAN_THREADS * ITEMS;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ int64_t s_tile;
+  __shared__ S s_warp[1][SCAN_THREADS / 32];
+  __shared__ S s_prefix;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const uint32_t dyn = atomicAdd(a.ticket, 1u);
+    // The holder of the last ticket knows every other CTA has taken its
+    // ticket: it re-arms the counter for the next launch on this stream.
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    s_tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t base = tile * (int64_t)TILE;
+  const T idT = Prim<OP, T>::id();
+  const T *src = static_cast<const T *>(a.in);
+  const T *src2 = static_cast<const T *>(a.in2);
+  (void)src2;
+  for (int e = tid; e < TILE; e += SCAN_THREADS) {
+    const int64_t gi = base + e;
+    T v = idT;
+    if (gi < a.n) {
+      if constexpr (ZIP) v = zip_elem(a.zop, src[gi], src2[gi]);
+      else v = src[gi];
+    }
+    const int r = e / ITEMS, k = e % ITEMS;
+    *reinterpret_cast<T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T)) = v;
+  }
+  __syncthreads();
+  scan_tile_body<OP, T, PREC, R2L, 1>(buf, tile, a, s_warp, s_prefix, true);
+  __syncthreads();
+  T *dst = static_cast<T *>(a.out);
+  for (int e = tid; e < TILE; e += SCAN_THREADS) {
+    const int64_t gi = base + e;
+    if (gi < a.n) {
+      const int r = e / ITEMS, k = e % ITEMS;
+      dst[gi] = *reinterpret_cast<const T *>(buf + swz(r, k / VEC) + (k % VEC) * sizeof(T));
+    }
+  }
+}
+
+// One tile (SUB x 32 KiB) per CTA through TMA, for 16-byte aligned arrays:
+// the tile arrives with SUB 2-D TMA loads of [256 rows x 128 B] on one
+// mbarrier, is scanned in shared memory, and leaves with SUB TMA stores.
+template <int OP, class T, int PREC, bool R2L, int SUB>
+__global__ void __launch_bounds__(SCAN_THREADS, SUB == 1 ? 6 : 3)
+scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+  using S = typename Acc<OP, T, PREC>::S;
+  constexpr int SUB_BYTES = SCAN_THREADS * SCAN_ROW_BYTES;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t bar;
+  __shared__ int64_t s_tile;
+  __shared__ S s_warp[SUB][SCAN_THREADS / 32];
+  __shared__ S s_prefix;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const uint32_t dyn = atomicAdd(a.ticket, 1u);
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    const int64_t tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
+    s_tile = tile;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_expect_tx(&bar, SUB * SUB_BYTES);
+#pragma unroll
+    for (int u = 0; u < SUB; ++u)
+      tma_load_2d(buf + u * SUB_BYTES, &tin, 0, (int)((tile * SUB + u) * SCAN_THREADS), &bar);
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  if (!mbar_wait(&bar, 0)) {
+    raise_error(a.err, DEV_ERR_TIMEOUT);
+    mbar_wait(&bar, 0);
+  }
+  // Each sub-tile leaves by TMA as soon as it is rescanned, while the next
+  // one is rescanned; the CTA waits only for the last store's reads.
+  auto store_sub = [&](int u) {
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tma_store_2d(&tout, 0, (int)((tile * SUB + u) * SCAN_THREADS), buf + u * SUB_BYTES);
+      tma_store_commit();
+    }
+  };
+  scan_tile_body<OP, T, PREC, R2L, SUB>(buf, tile, a, s_warp, s_prefix, false, store_sub);
+  if (tid == 0) tma_store_wait_read();
+}
+
+// Zip one thread's 128-byte row of the two swizzled tiles into the first:
+// buf[row] = g buf[row] buf2[row], element by element.
+template <class T, int Z>
+__device__ __forceinline__ void zip_row(unsigned char *buf, const unsigned char *buf2, int row) {
+  constexpr int VEC = 16 / sizeof(T);
+#pragma unroll
+  for (int c = 0; c < SCAN_ROW_BYTES / 16; ++c) {
+    uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(row, c));
+    const uint4 w = *reinterpret_cast<const uint4 *>(buf2 + swz(row, c));
+    T x[VEC], y[VEC];
+    memcpy(x, &v, 16);
+    memcpy(y, &w, 16);
+#pragma unroll
+    for (int k = 0; k < VEC; ++k) x[k] = Prim<Z, T>::ap(x[k], y[k]);
+    memcpy(&v, x, 16);
+    *reinterpret_cast<uint4 *>(buf + swz(row, c)) = v;
+  }
+}
+
+// scan f z (zipWith g xs ys) for 16-byte aligned xs, ys and output (the
+// reference's delayed scan input, PTX/CodeGen/Scan.hs:141-439 reading a
+// MIRDelayed array): one 32 KiB tile of xs and the same tile of ys arrive by
+// two 2-D TMA loads on one mbarrier, each thread zips its own row into the
+// xs buffer, and the zipped tile is scanned and stored as scan_tma_kernel
+// scans and stores one sub-tile.  The zipped array is never written; 64 KiB
+// of shared memory per CTA, three CTAs per SM.
+template <int OP, class T, int PREC, bool R2L>
+__global__ void __launch_bounds__(SCAN_THREADS, 3)
+scan_zip_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tin2,
+                    const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+  using S = typename Acc<OP, T, PREC>::S;
+  constexpr int SUB_BYTES = SCAN_THREADS * SCAN_ROW_BYTES;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *buf = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char *buf2 = buf + SUB_BYTES;
+  __shared__ uint64_t bar;
+  __shared__ int64_t s_tile;
+  __shared__ S s_warp[1][SCAN_THREADS / 32];
+  __shared__ S s_prefix;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    const uint32_t dyn = atomicAdd(a.ticket, 1u);
+    if ((int64_t)dyn == a.ntiles - 1) *a.ticket = 0u;
+    const int64_t tile = R2L ? a.ntiles - 1 - (int64_t)dyn : (int64_t)dyn;
+    s_tile = tile;
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    mbar_expect_tx(&bar, 2 * SUB_BYTES);
+    tma_load_2d(buf, &tin, 0, (int)(tile * SCAN_THREADS), &bar);
+    tma_load_2d(buf2, &tin2, 0, (int)(tile * SCAN_THREADS), &bar);
+  }
+  __syncthreads();
+  const int64_t tile = s_tile;
+  if (!mbar_wait(&bar, 0)) {
+    raise_error(a.err, DEV_ERR_TIMEOUT);
+    mbar_wait(&bar, 0);
+  }
+  // Rows past the array's full 128 B lines are read (and zipped) from global
+  // memory by the tile body.
+  if (tile * SCAN_THREADS + tid < a.full_rows) {
+    switch (a.zop) {
+      case ACC_ADD: zip_row<T, ACC_ADD>(buf, buf2, tid); break;
+      case ACC_MUL: zip_row<T, ACC_MUL>(buf, buf2, tid); break;
+      case ACC_MIN: zip_row<T, ACC_MIN>(buf, buf2, tid); break;
+      default: zip_row<T, ACC_MAX>(buf, buf2, tid); break;
+    }
+  }
+  auto store_sub = [&](int u) {
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tma_store_2d(&tout, 0, (int)((tile + u) * SCAN_THREADS), buf + u * SUB_BYTES);
+      tma_store_commit();
+    }
+  };
+  scan_tile_body<OP, T, PREC, R2L, 1, true>(buf, tile, a, s_warp, s_prefix, false, store_sub);
+  if (tid == 0) tma_store_wait_read();
+}
+
+// --------------------------------------------------------------------------
+// Row scans (rank >= 2): one CTA per row, chunks of 256 x 4 elements with a
+// carried prefix.  in/out rows have pitches in_pitch / out_pitch (elements).
+struct RowScanArgs {
+  const void *in;
+  void *out;
+  void *sums;        // per-row totals (scan') or null
+  int64_t outer, inner;
+  int64_t in_pitch, out_pitch;
+  int64_t out_shift; // 1 for scanl z (output index i+1 holds the inclusive prefix of i), else 0
+  uint64_t seed;
+  int has_seed;
+  int exclusive;
+  int seed_at_end;   // scanr z: out[row][inner] = z
+  int total_at_end;  // scanl z: out[row][inner] = total
+  const void *in2;   // ZIP kernels: element e of row r is zop(in[r][e], in2[r][e]) (pitch in_pitch)
+  int zop;
+};
+
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+__global__ void __launch_bounds__(256) scan_rows_kernel(RowScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  constexpr int K = 4;
+  constexpr int CH = 256 * K;
+  __shared__ S s_warp[8];
+  __shared__ S s_carry;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const T idT = Prim<OP, T>::id();
+  for (int64_t r = blockIdx.x; r < a.outer; r += gridDim.x) {
+    const T *src = static_cast<const T *>(a.in) + r * a.in_pitch;
+    const T *src2 = ZIP ? static_cast<const T *>(a.in2) + r * a.in_pitch : nullptr;
+    (void)src2;
+    T *dst = static_cast<T *>(a.out) + r * a.out_pitch;
+    if (tid == 0) s_carry = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
+    __syncthreads();
+    const int64_t nch = (a.inner + CH - 1) / CH;
+    for (int64_t ci = 0; ci < nch; ++ci) {
+      const int64_t c = R2L ? nch - 1 - ci : ci;
+      const int64_t e0 = c * CH + (int64_t)tid * K;
+      T x[K];
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        x[j] = idT;
+        if (e0 + j < a.inner) {
+          if constexpr (ZIP) x[j] = zip_elem(a.zop, src[e0 + j], src2[e0 + j]);
+          else x[j] = src[e0 + j];
+        }
+      }
+      S agg;
+      if (!R2L) { agg = A::lift(x[0]); for (int j = 1; j < K; ++j) agg = A::push(agg, x[j]); }
+      else { agg = A::lift(x[K - 1]); for (int j = K - 2; j >= 0; --j) agg = A::push(agg, x[j]); }
+      S incl, ex;
+      if (!R2L) {
+        incl = warp_scan_incl<A>(agg);
+        S up = shfl_up(incl, 1);
+        ex = lane == 0 ? A::id() : up;
+        if (lane == 31) s_warp[warp] = incl;
+      } else {
+        incl = warp_scan_incl_rev<A>(agg);
+        S dn = shfl_down(incl, 1);
+        ex = lane == 31 ? A::id() : dn;
+        if (lane == 0) s_warp[warp] = incl;
+      }
+      __syncthreads();
+      S wpre = A::id();
+      if (!R2L) { for (int w = 0; w < warp; ++w) wpre = A::comb(wpre, s_warp[w]); }
+      else { for (int w = warp + 1; w < 8; ++w) wpre = A::comb(wpre, s_warp[w]); }
+      S bagg = s_warp[0];
+      for (int w = 1; w < 8; ++w) bagg = A::comb(bagg, s_warp[w]);
+      const S carry = s_carry;
+      S run = R2L ? A::comb(A::comb(ex, wpre), carry) : A::comb(carry, A::comb(wpre, ex));
+      if (!R2L) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+          T yv;
+          if (a.exclusive) { yv = A::lower(run); run = A::push(run, x[j]); }
+          else { run = A::push(run, x[j]); yv = A::lower(run); }
+          if (e0 + j < a.inner) dst[e0 + j] = yv;
+        }
+      } else {
+#pragma unroll
+        for (int j = K - 1; j >= 0; --j) {
+          T yv;
+          if (a.exclusive) { yv = A::lower(run); run = A::push(run, x[j]); }
+          else { run = A::push(run, x[j]); yv = A::lower(run); }
+          if (e0 + j < a.inner) dst[e0 + j] = yv;
+        }
+      }
+      __syncthreads();
+      if (tid == 0) s_carry = R2L ? A::comb(bagg, carry) : A::comb(carry, bagg);
+      __syncthreads();
+    }
+    if (tid == 0) {
+      const T total = A::lower(s_carry);
+      if (a.sums) static_cast<T *>(a.sums)[r] = total;
+      if (a.total_at_end) dst[a.inner] = total;
+      if (a.seed_at_end) dst[a.inner] = from_bits<T>(a.seed);
+    }
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------- host side
+constexpr size_t SCAN_SMEM = SCAN_THREADS * SCAN_ROW_BYTES + 1024;
+
+template <int OP, class T, int PREC, bool R2L, int SUB>
+int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
+                       bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  CUtensorMap tin, tout;
+  memset(&tin, 0, sizeof(tin));
+  memset(&tout, 0, sizeof(tout));
+  const int64_t full_rows = n / ITEMS;
+  const bool tma = full_rows > 0 &&
+                   encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true) &&
+                   encode_2d(&tout, out, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
+  const int sub = tma ? SUB : 1;
+  const int64_t tile_elems = (int64_t)sub * SCAN_THREADS * ITEMS;
+  const int64_t ntiles = cdiv_h(n, tile_elems);
+  if (ntiles >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
+  int st = ws_status(w, (size_t)ntiles * 2);
+  if (st) return st;
+  ScanArgs a{};
+  a.in = in; a.out = out; a.total_out = total_out; a.seed_out = seed_out;
+  a.n = n;
+  a.full_rows = full_rows;
+  a.ntiles = ntiles;
+  a.seed = seed;
+  a.status = w->status;
+  a.ticket = w->words + W_TICKET;
+  a.err = w->words + W_ERR;
+  a.epoch = ws_next_epoch(w, s);
+  a.has_seed = has_seed;
+  a.exclusive = exclusive;
+  a.tma_in = a.tma_out = tma;
+  if (tma) {
+    const size_t smem = (size_t)SUB * SCAN_THREADS * SCAN_ROW_BYTES + 1024;
+    auto kern = scan_tma_kernel<OP, T, PREC, R2L, SUB>;
+    static std::atomic<uint64_t> attr_done{0};
+    smem_attrs_once(kern, (int)smem, attr_done);
+    kern<<<(unsigned)ntiles, SCAN_THREADS, smem, s>>>(tin, tout, a);
+    return check_launch();
+  }
+  auto kern = scan_lookback_kernel<OP, T, PREC, R2L>;
+  static std::atomic<uint64_t> attr_done{0};
+  smem_attrs_once(kern, (int)SCAN_SMEM, attr_done);
+  kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(a);
+  return check_launch();
+}
+
+// Tile size: 2 sub-tiles (64 KiB, 3 CTAs per SM) by default, the faster of
+// the two on GB300 at 2^25..2^28 elements; ACC_GB300_SCAN_SUB=1 selects 32 KiB
+// tiles (6 CTAs per SM).
+template <int OP, class T, int PREC, bool R2L>
+int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
+                   bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+  static const int sub = getenv("ACC_GB300_SCAN_SUB") ? atoi(getenv("ACC_GB300_SCAN_SUB")) : 2;
+  if (sub == 2)
+    return launch_scan_1d_sub<OP, T, PREC, R2L, 2>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
+  return launch_scan_1d_sub<OP, T, PREC, R2L, 1>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
+}
+
+// Short rows, many of them: one warp per row.  The warp walks the row in
+// chunks of 32 elements (one per lane, coalesced), scans each chunk with
+// shuffles and carries the prefix in a register; the semantics are those of
+// scan_rows_kernel (seed placement, exclusive flavours, totals).
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+__global__ void __launch_bounds__(256) scan_rows_warp_kernel(RowScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  const int lane = threadIdx.x & 31;
+  const T idT = Prim<OP, T>::id();
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = gw; r < a.outer; r += nw) {
+    const T *src = static_cast<const T *>(a.in) + r * a.in_pitch;
+    const T *src2 = ZIP ? static_cast<const T *>(a.in2) + r * a.in_pitch : nullptr;
+    (void)src2;
+    T *dst = static_cast<T *>(a.out) + r * a.out_pitch;
+    S carry = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
+    const int64_t nch = (a.inner + 31) / 32;
+    for (int64_t ci = 0; ci < nch; ++ci) {
+      const int64_t c = R2L ? nch - 1 - ci : ci;
+      const int64_t e = c * 32 + lane;
+      T x = idT;
+      if (e < a.inner) {
+        if constexpr (ZIP) x = zip_elem(a.zop, src[e], src2[e]);
+        else x = src[e];
+      }
+      const S v = A::lift(x);
+      S incl, ex, tot;
+      if (!R2L) {
+        incl = warp_scan_incl<A>(v);
+        const S up = shfl_up(incl, 1);
+        ex = lane == 0 ? A::id() : up;
+        tot = shfl_idx(incl, 31);
+      } else {
+        incl = warp_scan_incl_rev<A>(v);
+        const S dn = shfl_down(incl, 1);
+        ex = lane == 31 ? A::id() : dn;
+        tot = shfl_idx(incl, 0);
+      }
+      // Everything before (L2R) / after (R2L) this element within the row.
+      const S before = R2L ? A::comb(ex, carry) : A::comb(carry, ex);
+      const T yv = a.exclusive ? A::lower(before) : A::lower(A::push(before, x));
+      if (e < a.inner) dst[e] = yv;
+      carry = R2L ? A::comb(tot, carry) : A::comb(carry, tot);
+    }
+    if (lane == 0) {
+      const T total = A::lower(carry);
+      if (a.sums) static_cast<T *>(a.sums)[r] = total;
+      if (a.total_at_end) dst[a.inner] = total;
+      if (a.seed_at_end) dst[a.inner] = from_bits<T>(a.seed);
+    }
+  }
+}
+
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+int launch_scan_rows(const RowScanArgs &a, cudaStream_t s) {
+  const Device &d = device_info();
+  if (a.inner <= 512 && a.outer >= (int64_t)d.sms * 64) {
+    // a warp per row: 8 rows per CTA
+    int64_t blocks = cdiv_h(a.outer, 8);
+    if (blocks > (int64_t)d.sms * 16) blocks = (int64_t)d.sms * 16;
+    scan_rows_warp_kernel<OP, T, PREC, R2L, ZIP><<<(unsigned)blocks, 256, 0, s>>>(a);
+    return check_launch();
+  }
+  int64_t blocks = a.outer;
+  if (blocks > (int64_t)d.sms * 8) blocks = (int64_t)d.sms * 8;
+  scan_rows_kernel<OP, T, PREC, R2L, ZIP><<<(unsigned)blocks, 256, 0, s>>>(a);
+  return check_launch();
+}
+
+// A 1-D scan over zipWith g in in2 (g = zop): the zipped tile kernel when
+// the three arrays are 16-byte aligned, else the plain-load look-back kernel
+// zipping as it loads.  Tiles of 32 KiB in both cases.
+template <int OP, class T, int PREC, bool R2L>
+int launch_scan_zip_1d(Workspace *w, const T *in, const T *in2, int zop, T *out, T *total_out, T *seed_out,
+                       int64_t n, bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  CUtensorMap tin, tin2, tout;
+  memset(&tin, 0, sizeof(tin));
+  memset(&tin2, 0, sizeof(tin2));
+  memset(&tout, 0, sizeof(tout));
+  const int64_t full_rows = n / ITEMS;
+  const bool tma = full_rows > 0 &&
+                   encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true) &&
+                   encode_2d(&tin2, in2, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true) &&
+                   encode_2d(&tout, out, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
+  const int64_t ntiles = cdiv_h(n, (int64_t)SCAN_THREADS * ITEMS);
+  if (ntiles >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
+  int st = ws_status(w, (size_t)ntiles * 2);
+  if (st) return st;
+  ScanArgs a{};
+  a.in = in; a.out = out; a.total_out = total_out; a.seed_out = seed_out;
+  a.in2 = in2; a.zop = zop;
+  a.n = n;
+  a.full_rows = full_rows;
+  a.ntiles = ntiles;
+  a.seed = seed;
+  a.status = w->status;
+  a.ticket = w->words + W_TICKET;
+  a.err = w->words + W_ERR;
+  a.epoch = ws_next_epoch(w, s);
+  a.has_seed = has_seed;
+  a.exclusive = exclusive;
+  a.tma_in = a.tma_out = tma;
+  if (tma) {
+    const size_t smem = 2 * (size_t)SCAN_THREADS * SCAN_ROW_BYTES + 1024;
+    auto kern = scan_zip_tma_kernel<OP, T, PREC, R2L>;
+    static std::atomic<uint64_t> attr_done{0};
+    smem_attrs_once(kern, (int)smem, attr_done);
+    kern<<<(unsigned)ntiles, SCAN_THREADS, smem, s>>>(tin, tin2, tout, a);
+    return check_launch();
+  }
+  auto kern = scan_lookback_kernel<OP, T, PREC, R2L, true>;
+  static std::atomic<uint64_t> attr_done{0};
+  smem_attrs_once(kern, (int)SCAN_SMEM, attr_done);
+  kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(a);
+  return check_launch();
+}
+
+// Every scan flavour over one array, or (ZIP) over zipWith g in in2 with
+// g = zop, both [outer x inner].
+template <int OP, class T, int PREC, bool ZIP = false>
+int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, int64_t outer,
+               int64_t inner, uint64_t seed, cudaStream_t s, const T *in2 = nullptr, int zop = 0) {
+  const bool r2l = dir == ACC_R2L;
+  const bool seeded = kind != ACC_SCAN_INCLUSIVE;
+  // Empty innermost extent: scanl/scanr z give [z]; scanl'/scanr' give
+  // ([], z); scanl1/scanr1 give [] (PTX/Execute.hs:386-404,500-512).
+  if (inner == 0) {
+    if (kind == ACC_SCAN_SEEDED) return launch_fill<T>(out, outer, seed, s);
+    if (kind == ACC_SCAN_PRIME) return launch_fill<T>(sums, outer, seed, s);
+    return ACC_OK;
+  }
+  // Output element i lines up with input element i in every flavour:
+  //   scanl z  (L2R, exclusive, total -> out[n])
+  //   scanr z  (R2L, inclusive with the seed on the right, z -> out[n])
+  //   scanl' z (L2R, exclusive, total -> sums), scanr' z (R2L, exclusive, total -> sums)
+  const bool exclusive = kind == ACC_SCAN_PRIME || (kind == ACC_SCAN_SEEDED && !r2l);
+  if (outer == 1) {
+    T *total_out = nullptr, *seed_out = nullptr;
+    if (kind == ACC_SCAN_SEEDED && !r2l) total_out = out + inner;
+    if (kind == ACC_SCAN_SEEDED && r2l) seed_out = out + inner;
+    if (kind == ACC_SCAN_PRIME) total_out = sums;
+    if constexpr (ZIP) {
+      if (r2l)
+        return launch_scan_zip_1d<OP, T, PREC, true>(w, in, in2, zop, out, total_out, seed_out, inner, seeded,
+                                                     exclusive, seed, s);
+      return launch_scan_zip_1d<OP, T, PREC, false>(w, in, in2, zop, out, total_out, seed_out, inner, seeded,
+                                                    exclusive, seed, s);
+    } else {
+      (void)in2;
+      (void)zop;
+      if (r2l) return launch_scan_1d<OP, T, PREC, true>(w, in, out, total_out, seed_out, inner, seeded, exclusive, seed, s);
+      return launch_scan_1d<OP, T, PREC, false>(w, in, out, total_out, seed_out, inner, seeded, exclusive, seed, s);
+    }
+  }
+  RowScanArgs a{};
+  a.in = in; a.out = out; a.sums = kind == ACC_SCAN_PRIME ? sums : nullptr;
+  a.outer = outer; a.inner = inner;
+  a.in_pitch = inner;
+  a.out_pitch = kind == ACC_SCAN_SEEDED ? inner + 1 : inner;
+  a.seed = seed; a.has_seed = seeded; a.exclusive = exclusive;
+  a.seed_at_end = kind == ACC_SCAN_SEEDED && r2l;
+  a.total_at_end = kind == ACC_SCAN_SEEDED && !r2l;
+  a.in2 = in2; a.zop = zop;
+  if (r2l) return launch_scan_rows<OP, T, PREC, true, ZIP>(a, s);
+  return launch_scan_rows<OP, T, PREC, false, ZIP>(a, s);
+}
+
+}  // namespace accgb

@@ -11,7 +11,7 @@ seeded synthetic data of the workload's shapes and distributions, generated
 on the device; every input is larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --only scan|fold|permute|stencil|foldseg|batched|dotp [--scale S]   (one kernel, small case)
+  python bench.py --only scan|fold|permute|stencil|foldseg|batched|dotp|scanzip [--scale S]   (one kernel, small case)
 
 `--impl reference` times the CPU restatement of accelerate-llvm-native (the
 reference's own CPU backend cannot be built here) on all host cores over a
@@ -595,6 +595,19 @@ def run_only(args):
         xs = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
         ys = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
         fn, nbytes = (lambda: acc.dotp(xs, ys)), 8 * xs.numel()
+    elif name == "scanzip":
+        # scanl1 (+) (zipWith (*) xs ys) on Float32 with the zipWith fused into
+        # the scan: 12 B/element (two reads, one write)
+        g = torch.Generator(device=dev)
+        g.manual_seed(SEED + 10)
+        xs = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
+        ys = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
+        zout = acc.scan_zipwith("scanl1", "+", "*", None, xs, ys)
+        ref = torch.cumsum(xs.double() * ys.double(), 0)
+        err = float(((zout.double() - ref).abs() / torch.cumsum((xs.double() * ys.double()).abs(), 0)).max())
+        assert err < 1e-6, f"scanl1 (+) (zipWith (*)) error {err}"
+        del ref
+        fn, nbytes = (lambda: acc.scan_zipwith("scanl1", "+", "*", None, xs, ys)), 12 * xs.numel()
     else:
         inp = make_inputs(torch, dev, args.scale)
         zeros = torch.zeros(M_PERM, dtype=torch.int32, device=dev)
@@ -868,7 +881,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch workload")
     ap.add_argument("--serve-seconds", type=float, default=3.0,
                     help="length of the 20k req/s serving stream (0: skip serving)")
-    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp"],
+    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp", "scanzip"],
                     help="time one skeleton alone (small-case driver for ncu captures)")
     ap.add_argument("--scale", type=int, default=1, help="with --only: 1/scale of the full input")
     args = ap.parse_args()

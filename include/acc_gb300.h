@@ -195,6 +195,19 @@ int acc_scan(int op, int type, int prec, int dir, int kind, const void *in,
              void *out, void *sums, int64_t outer, int64_t inner,
              const void *seed, void *stream);
 
+/* Every scan flavour of acc_scan over the fused producer zipWith g xs ys,
+ * e.g. scanl1 (+) (zipWith (*) xs ys).  Replaces scanOp / scan1Op / scan'Op
+ * on a delayed zipWith input (PTX/CodeGen/Scan.hs:141-439 and 746-939, the
+ * MIRDelayed argument of the scan kernels): the zipped array is never
+ * written.  xs, ys: outer*inner elements each, same layout; every zipped
+ * element is g x y rounded to `type`; out / sums / seed / dir / kind as for
+ * acc_scan.  op in {ADD, MIN, MAX}, zop in {ADD, MUL, MIN, MAX}, type in
+ * {I32, I64, F32, F64}; other combinations give ACC_ERR_UNSUPPORTED. */
+int acc_scan_zipwith(int op, int zop, int type, int prec, int dir, int kind,
+                     const void *xs, const void *ys, void *out, void *sums,
+                     int64_t outer, int64_t inner, const void *seed,
+                     void *stream);
+
 /* acc_scan without any device allocation -- no counterpart in the reference,
  * which always allocates its temporaries (PTX/Execute.hs:453).  Same
  * arguments, results and errors as acc_scan, for callers that cannot let a

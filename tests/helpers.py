@@ -10,7 +10,16 @@ Comparison rules (the tolerances are written here, once):
     1.0, a sparse 0.5 / 2.0), whose products are exact in any order: a
     coverage check that every element is combined exactly once.
 """
+import zlib
+
 import numpy as np
+
+
+def case_rng(*parts):
+    """A generator seeded from the test case's parameters, the same in every
+    run and on every machine (unlike hash(), which Python randomises per
+    process), so that a failing case can be rerun on the same data."""
+    return np.random.default_rng(zlib.crc32(repr(parts).encode()))
 
 TYPES = {"i32": np.int32, "i64": np.int64, "u32": np.uint32, "f32": np.float32, "f64": np.float64}
 INT_OPS = ["+", "*", "min", "max", "and", "or", "xor"]

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import seed_for
+from helpers import case_rng, seed_for
 
 pytestmark = pytest.mark.gpu
 
@@ -59,7 +59,7 @@ def check(got, ref, xs, f):
 
 @pytest.mark.parametrize("f", ["+", "min", "max"])
 def test_batch_matches_per_call(acc, dev, f):
-    rng = np.random.default_rng(hash(f) & 0xFFFF)
+    rng = case_rng("batch", f)
     reqs, refs = make_requests(dev, f, rng)
     b = acc.Batch(f, reqs)
     b.launch()

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import COMBOS, TYPES, assert_fold_close, gen, seed_for
+from helpers import COMBOS, TYPES, assert_fold_close, case_rng, gen, seed_for
 
 pytestmark = pytest.mark.gpu
 
@@ -13,7 +13,7 @@ SHAPES = [(1, 1), (1, 5), (1, 17), (3, 100), (1, 100_003), (4096, 1024), (5000, 
 
 def run_fold(acc, orc, dev, t, op, shape, seeded, prec=None, offset=0):
     dt = TYPES[t]
-    rng = np.random.default_rng(hash((t, op, shape, seeded, offset)) & 0xFFFFFFFF)
+    rng = case_rng("fold", t, op, shape, seeded, offset)
     n = int(np.prod(shape))
     x = gen(dt, op, n + offset, rng)
     xs = x[offset:].reshape(shape)

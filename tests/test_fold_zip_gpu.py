@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import TYPES, assert_fold_close, gen, seed_for
+from helpers import TYPES, assert_fold_close, case_rng, gen, seed_for
 
 pytestmark = pytest.mark.gpu
 
@@ -36,7 +36,7 @@ def inputs(dt, f, g, n, rng):
 
 def run_zip(acc, orc, dev, t, f, g, shape, seeded, offset=0, prec=None):
     dt = TYPES[t]
-    rng = np.random.default_rng(hash((t, f, g, shape, seeded, offset)) & 0xFFFFFFFF)
+    rng = case_rng("fold_zip", t, f, g, shape, seeded, offset)
     n = int(np.prod(shape))
     x, y = inputs(dt, f, g, n + offset, rng)
     xs, ys = x[:n].reshape(shape), y[offset:].reshape(shape)

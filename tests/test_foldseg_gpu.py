@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import COMBOS, TYPES, _diff, assert_fold_close, gen, seed_for
+from helpers import COMBOS, TYPES, _diff, assert_fold_close, case_rng, gen, seed_for
 
 pytestmark = pytest.mark.gpu
 
@@ -19,7 +19,7 @@ def segmentation(rng, nseg, long_frac=0.01, zero_frac=0.05, maxlen=20_000):
 
 def run_seg(acc, orc, dev, t, op, nseg, seeded, outer=1, off_t=np.int32, prec=None, lengths_api=False):
     dt = TYPES[t]
-    rng = np.random.default_rng(hash((t, op, nseg, seeded, outer, str(off_t), lengths_api)) & 0xFFFFFFFF)
+    rng = case_rng("foldseg", t, op, nseg, seeded, outer, str(off_t), lengths_api)
     lens = segmentation(rng, nseg)
     off = np.concatenate([[0], np.cumsum(lens)]).astype(off_t)
     inner = int(off[-1])

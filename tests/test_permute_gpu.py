@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import COMBOS, TYPES, _diff, gen
+from helpers import COMBOS, TYPES, _diff, case_rng, gen
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +18,7 @@ def zipf_bins(rng, n, m, s=1.1):
 
 def run_perm(acc, orc, dev, t, op, n, m, const=False, idx_t=np.int32, drop=True):
     dt = TYPES[t]
-    rng = np.random.default_rng(hash((t, op, n, m, const, str(idx_t))) & 0xFFFFFFFF)
+    rng = case_rng("permute", t, op, n, m, const, str(idx_t))
     idx = rng.integers(-3 if drop else 0, m, size=n).astype(idx_t)
     xs = None if const else gen(dt, op, n, rng)
     defaults = gen(dt, op, m, rng)

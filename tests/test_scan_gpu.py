@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import COMBOS, TYPES, _diff, gen, seed_for
+from helpers import COMBOS, TYPES, _diff, case_rng, gen, seed_for
 
 pytestmark = pytest.mark.gpu
 
@@ -54,7 +54,7 @@ def _nan_equal(a, b):
 
 def run_scan(acc, orc, dev, t, op, shape, d, k, offset=0):
     dt = TYPES[t]
-    rng = np.random.default_rng(hash((t, op, shape, d, k, offset)) & 0xFFFFFFFF)
+    rng = case_rng("scan", t, op, shape, d, k, offset)
     n = int(np.prod(shape))
     x = gen(dt, op, n + offset, rng)
     xs = x[offset:].reshape(shape)

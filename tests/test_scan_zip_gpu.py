@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import TYPES, gen, seed_for
+from helpers import TYPES, case_rng, gen, seed_for
 from test_fold_zip_gpu import zipped
 from test_scan_gpu import FLAVOURS, NAMES, check_scan
 
@@ -21,7 +21,7 @@ ZIP_OPS = ["+", "*", "min", "max"]
 
 def run_scan_zip(acc, orc, dev, t, f, g, shape, d, k, offset=0, prec=None):
     dt = TYPES[t]
-    rng = np.random.default_rng(hash((t, f, g, shape, d, k, offset)) & 0xFFFFFFFF)
+    rng = case_rng("scan_zip", t, f, g, shape, d, k, offset)
     n = int(np.prod(shape))
     src = g if g == "*" else f
     x = gen(dt, src, n, rng)

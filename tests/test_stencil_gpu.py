@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import _diff
+from helpers import _diff, case_rng
 
 pytestmark = pytest.mark.gpu
 
@@ -34,7 +34,7 @@ def weights(dt, ry, rx, rng):
 @pytest.mark.parametrize("ry,rx", RADII)
 def test_stencil_grid(acc, orc, dev, t, b, ry, rx):
     dt = STYPES[t]
-    rng = np.random.default_rng(hash((t, b, ry, rx)) & 0xFFFFFFFF)
+    rng = case_rng("stencil", t, b, ry, rx)
     for shape in SHAPES:
         if shape[0] == 1 and ry > 0:
             continue

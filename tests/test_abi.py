@@ -59,3 +59,14 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_stencil2d(3, 5, 1, N, 0, N, N, N, 4, 4, N) == 1         # radius > 4
     assert lib.acc_stencil2d(2, 1, 1, N, 0, N, N, N, 4, 4, N) == 2         # Word32 stencil unsupported
     assert lib.acc_fold_seg(0, 0, 0, N, N, 3, N, 1, 4, 2, N, N) == 1       # bad offset type
+    # the fused zipWith entry points
+    out = ctypes.c_void_p(16)
+    assert lib.acc_fold_zipwith(0, 9, 0, 0, N, N, out, 1, 4, N, N) == 1    # bad zip primitive
+    assert lib.acc_fold_zipwith(0, 1, 0, 0, N, N, out, 2, 0, N, N) == 3    # fold1 of an empty row
+    assert lib.acc_fold_zipwith(0, 1, 0, 0, N, N, out, 1, 4, N, N) == 1    # missing inputs
+    assert lib.acc_scan_zipwith(0, 9, 0, 0, 0, 0, N, N, out, N, 1, 4, N, N) == 1  # bad zip primitive
+    assert lib.acc_scan_zipwith(0, 1, 0, 0, 7, 0, N, N, out, N, 1, 4, N, N) == 1  # bad direction
+    assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 1, N, N, out, N, 1, 4, N, N) == 1  # scanl without seed
+    assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 0, N, N, out, N, 1, 4, N, N) == 1  # missing inputs
+    assert lib.acc_scan_zipwith(0, 4, 0, 0, 0, 0, out, out, out, N, 1, 4, N, N) == 2  # zipWith (.&.) unsupported
+    assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 2, out, out, out, N, 1, 4, out, N) == 1  # scanl' without sums

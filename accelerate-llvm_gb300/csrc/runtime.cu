@@ -64,6 +64,12 @@ Workspace *workspace(cudaStream_t s, int *status) {
   Workspace *raw = w.get();
   g_ws.emplace(key, std::move(w));
   *status = ws_words(raw, 64);
+  if (*status != ACC_OK) {
+    // No control words (ticket, error word): the workspace is unusable, so it
+    // is not kept for the next call on this stream either.
+    g_ws.erase(key);
+    return nullptr;
+  }
   return raw;
 }
 

@@ -28,6 +28,14 @@ def test_known_answer_scanl_example(orc):
     assert out.tolist() == g["expect"] and out.size == g["out_len"]
 
 
+def test_known_answer_scanl_prime_example(orc):
+    # mkScan's example of scanl' (exclusive scan, total returned apart)
+    g = GOLDEN["scanl_prime_example"]
+    xs = np.array(g["input"], dtype=np.int64)
+    out, tot = orc.scan(g["op"], g["seed"], xs, 0, 2)
+    assert out.tolist() == g["expect"] and out.size == g["out_len"] and int(tot) == g["expect_total"]
+
+
 def test_scan_flavours_small(orc):
     xs = np.arange(10, dtype=np.int64)
     # scanr z: out[i] = x_i + ... + x_(n-1) + z, out[n] = z (Native/CodeGen/Scan.hs:190-205)

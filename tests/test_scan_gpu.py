@@ -108,6 +108,9 @@ def test_scan_known_answer(acc, dev):
     # scanl (+) 10 [0..9] (Native/CodeGen/Scan.hs:50-56)
     xs = torch.arange(10, dtype=torch.int64, device=dev)
     assert acc.scanl("+", 10, xs).cpu().tolist() == [10, 10, 11, 13, 16, 20, 25, 31, 38, 46, 55]
+    # mkScan's scanl' example (Native/CodeGen/Scan.hs:78-85)
+    out, tot = acc.scanl_("+", 10, xs)
+    assert out.cpu().tolist() == [10, 10, 11, 13, 16, 20, 25, 31, 38, 46] and int(tot.item()) == 55
     out, tot = acc.scanr_("+", 10, xs)
     assert out.cpu().tolist() == [55, 54, 52, 49, 45, 40, 34, 27, 19, 10] and int(tot.item()) == 55
 

@@ -786,18 +786,21 @@ def cpu_bytes(scale, h):
             "permute": 4 * (N_PERM // scale) + 8 * M_PERM, "stencil": 8 * h * h}
 
 
+CPU_RUNS = 5  # the CPU baseline is the median of this many runs after one warm-up
+
+
 def cpu_baseline(scale):
     import oracle
     nth = os.cpu_count() or 1
     inp = cpu_inputs(scale)
     cpu_step(oracle, inp, nth)
-    runs = [cpu_step(oracle, inp, nth) for _ in range(3)]
+    runs = [cpu_step(oracle, inp, nth) for _ in range(CPU_RUNS)]
     sec = {k: statistics.median(r[k] for r in runs) for k in runs[0]}
     b = cpu_bytes(scale, inp["h"])
     return {"value": round(sum(b.values()) / sum(sec.values()) / 1e9, 2), "unit": "GB/s", "cores": nth,
             "kind": "port",
             "sample": f"1/{scale} of each input (scan {N_SCAN // scale}, fold {N_FOLD // scale}, permute "
-                      f"{N_PERM // scale} -> 2^16, stencil {inp['h']}^2); median of 3 after 1 warm-up",
+                      f"{N_PERM // scale} -> 2^16, stencil {inp['h']}^2); median of {CPU_RUNS} after 1 warm-up",
             "per_skeleton_gbs": {k: round(b[k] / sec[k] / 1e9, 2) for k in sec}}
 
 

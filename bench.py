@@ -789,6 +789,25 @@ def cpu_bytes(scale, h):
 CPU_RUNS = 5  # the CPU baseline is the median of this many runs after one warm-up
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in pathlib.Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_baseline(scale):
     import oracle
     nth = os.cpu_count() or 1
@@ -798,7 +817,7 @@ def cpu_baseline(scale):
     sec = {k: statistics.median(r[k] for r in runs) for k in runs[0]}
     b = cpu_bytes(scale, inp["h"])
     return {"value": round(sum(b.values()) / sum(sec.values()) / 1e9, 2), "unit": "GB/s", "cores": nth,
-            "kind": "port",
+            "cpu": cpu_model(), "kind": "port",
             "sample": f"1/{scale} of each input (scan {N_SCAN // scale}, fold {N_FOLD // scale}, permute "
                       f"{N_PERM // scale} -> 2^16, stencil {inp['h']}^2); median of {CPU_RUNS} after 1 warm-up",
             "per_skeleton_gbs": {k: round(b[k] / sec[k] / 1e9, 2) for k in sec}}
@@ -824,7 +843,7 @@ def run_reference(args):
         "config": {"workload": "scanl1 (+) Int64 2^28; fold (+) Float32 2^28; permute (+) histogram 2^28 Int32 "
                                "Zipf(1.1) -> 2^16 bins; stencil 3x3 Float32 8192^2 clamp",
                    "sample": f"1/{scale} of each input per step"},
-        "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": nth, "kind": "port",
+        "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": nth, "cpu": cpu_model(), "kind": "port",
                          "sample": f"1/{scale} of each input per step"},
         "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "per_skeleton_gbs": {k: round(b[k] * args.steps / sum(r[k] for r in runs) / 1e9, 2) for k in b},

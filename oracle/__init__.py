@@ -62,6 +62,7 @@ def lib():
             "orc_fold_seg_f64": ([I, I, P, P, I, P, L, L, L, P], I),
             "orc_scan_f64": ([I, I, I, I, P, P, P, L, L, P], I),
             "orc_stencil2d": ([I, I, I, P, I, P, P, L, L, P, L, L, I, I], I),
+            "orc_stencil3d": ([I, I, I, I, P, I, P, P, L, L, L, P, L, L, L, I, I], I),
         }
         for k, (a, r) in sig.items():
             f = getattr(_lib, k)
@@ -215,4 +216,29 @@ def stencil2d(weights, xs, boundary: int = 0, cval=None, nthreads: int = 1, accu
     cp, keep = _scalar(xs.dtype, 0 if cval is None else cval)
     _chk(lib().orc_stencil2d(CODE_OF[xs.dtype], ky // 2, kx // 2, _p(w2), boundary, cp, _p(xs), ih, iw, _p(out), h,
                              w, acc, nthreads))
+    return out
+
+
+def stencil3d(weights, xs, boundary: int = 0, cval=None, nthreads: int = 1, accumulate_onto=None,
+              out_shape=None) -> np.ndarray:
+    """Weighted-sum stencil of a rank-3 array [planes][rows][columns] with a
+    (2rz+1) x (2ry+1) x (2rx+1) weight array; taps planes outer, rows, then
+    columns, every index component remapped by the boundary.  accumulate_onto
+    and out_shape as for stencil2d."""
+    xs = np.ascontiguousarray(xs)
+    w3 = np.ascontiguousarray(np.asarray(weights, dtype=xs.dtype))
+    if xs.ndim != 3 or w3.ndim != 3:
+        raise ValueError("stencil3d takes a rank-3 array and a rank-3 weight pattern")
+    kz, ky, kx = w3.shape
+    if out_shape is None:
+        out_shape = xs.shape
+    if accumulate_onto is not None:
+        out = np.array(accumulate_onto, copy=True)
+        acc = 1
+    else:
+        out = np.empty(out_shape, dtype=xs.dtype)
+        acc = 0
+    cp, keep = _scalar(xs.dtype, 0 if cval is None else cval)
+    _chk(lib().orc_stencil3d(CODE_OF[xs.dtype], kz // 2, ky // 2, kx // 2, _p(w3), boundary, cp, _p(xs), *xs.shape,
+                             _p(out), *out_shape, acc, nthreads))
     return out

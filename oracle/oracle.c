@@ -37,18 +37,22 @@
  *    (CodeGen/Stencil.hs:195-253).  The stencil function is a weighted sum
  *    accumulated from the additive identity in tap order, one fused
  *    multiply-add per tap (C99 fma); zero-weight taps are not part of the
- *    pattern.
+ *    pattern.  A rank-3 pattern is a tuple of rank-2 patterns over the
+ *    outermost index (StencilRtup*, CodeGen/Stencil.hs:126-180, which recurse
+ *    on the left-most index component), so its taps run planes outer, then
+ *    rows, then columns; the boundary remaps every index component alike.
  *
  * Besides the restatement in the element type, *_f64 variants compute float
  * folds / scans / segmented folds in FP64 with Neumaier compensation: the
  * FP64 oracle against which Float32 errors are stated.
  *
- * Parity pins: the reference ships two known answers for this path,
+ * Parity pins: the reference ships three known answers for this path,
  * `sum (map (+1) [1..10000]) == 50015000` (accelerate-llvm-ptx/test/nofib/
- * Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs:26-31) and
+ * Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs:26-31),
  * `scanl (+) 10 [0..9] == [10,10,11,13,16,20,25,31,38,46,55]`
- * (accelerate-llvm-native/.../Native/CodeGen/Scan.hs:50-56); tests/ checks
- * this oracle against both.  The core package's property suite is not in the
+ * (accelerate-llvm-native/.../Native/CodeGen/Scan.hs:50-56) and the scanl'
+ * example of mkScan', ([10,10,11,13,16,20,25,31,38,46], 55) (the same file,
+ * :78-85); tests/ checks this oracle against all three.  The core package's property suite is not in the
  * tree, so the other (op, type, skeleton) cases are pinned only by this
  * restatement: parity partially pinned.
  */
@@ -516,6 +520,57 @@ DEFINE_STENCIL(f32, float, float, T_F32, -0.0f)
 DEFINE_STENCIL(f64, double, double, T_F64, -0.0)
 DEFINE_STENCIL(i32, int32_t, uint32_t, T_I32, 0)
 DEFINE_STENCIL(i64, int64_t, uint64_t, T_I64, 0)
+
+/* Rank 3: input [id][ih][iw], output [d][h][wd]; taps dz outer, dy, dx inner. */
+#define DEFINE_STENCIL3(NAME, T, TAP, ID)                                                                     \
+  static void NAME##_stencil3(int rz, int ry, int rx, const T *w, int b, const T *cval, const T *in,          \
+                              int64_t id, int64_t ih, int64_t iw, T *out, int64_t d, int64_t h, int64_t wd,   \
+                              int accumulate, int nth) {                                                      \
+    const int ky = 2 * ry + 1, kx = 2 * rx + 1;                                                               \
+    _Pragma("omp parallel for collapse(2) schedule(static) if (nth > 1)")                                     \
+    for (int64_t z = 0; z < d; ++z)                                                                           \
+      for (int64_t y = 0; y < h; ++y)                                                                         \
+        for (int64_t x = 0; x < wd; ++x) {                                                                    \
+          const int64_t o = (z * h + y) * wd + x;                                                             \
+          T acc = accumulate ? out[o] : (ID);                                                                 \
+          for (int dz = -rz; dz <= rz; ++dz)                                                                  \
+            for (int dy = -ry; dy <= ry; ++dy)                                                                \
+              for (int dx = -rx; dx <= rx; ++dx) {                                                            \
+                const T wk = w[((dz + rz) * ky + (dy + ry)) * kx + (dx + rx)];                                \
+                if (wk == 0) continue;                                                                        \
+                const int64_t zz = z + dz, yy = y + dy, xx = x + dx;                                          \
+                T v;                                                                                          \
+                if (zz >= 0 && zz < id && yy >= 0 && yy < ih && xx >= 0 && xx < iw)                          \
+                  v = in[(zz * ih + yy) * iw + xx];                                                           \
+                else if (b == 3) v = *cval;                                                                   \
+                else v = in[(bound_ix(zz, id, b) * ih + bound_ix(yy, ih, b)) * iw + bound_ix(xx, iw, b)];     \
+                acc = TAP(wk, v, acc);                                                                        \
+              }                                                                                               \
+          out[o] = acc;                                                                                       \
+        }                                                                                                     \
+  }
+DEFINE_STENCIL3(f32, float, T_F32, -0.0f)
+DEFINE_STENCIL3(f64, double, T_F64, -0.0)
+DEFINE_STENCIL3(i32, int32_t, T_I32, 0)
+DEFINE_STENCIL3(i64, int64_t, T_I64, 0)
+
+int orc_stencil3d(int type, int rz, int ry, int rx, const void *w, int boundary, const void *cval, const void *in,
+                  int64_t id, int64_t ih, int64_t iw, void *out, int64_t d, int64_t h, int64_t wd, int accumulate,
+                  int nth) {
+  if (rz < 0 || rz > 4 || ry < 0 || ry > 4 || rx < 0 || rx > 4 || boundary < 0 || boundary > 3 || d < 0 || h < 0 ||
+      wd < 0)
+    return E_INVALID;
+  if (boundary == 3 && !cval) return E_INVALID;
+  if ((d > 0 && d > id) || (h > 0 && h > ih) || (wd > 0 && wd > iw)) return E_INVALID;
+  switch (type) {
+    case T_F32: f32_stencil3(rz, ry, rx, w, boundary, cval, in, id, ih, iw, out, d, h, wd, accumulate, nth); break;
+    case T_F64: f64_stencil3(rz, ry, rx, w, boundary, cval, in, id, ih, iw, out, d, h, wd, accumulate, nth); break;
+    case T_I32: i32_stencil3(rz, ry, rx, w, boundary, cval, in, id, ih, iw, out, d, h, wd, accumulate, nth); break;
+    case T_I64: i64_stencil3(rz, ry, rx, w, boundary, cval, in, id, ih, iw, out, d, h, wd, accumulate, nth); break;
+    default: return E_UNSUPPORTED;
+  }
+  return OK;
+}
 
 int orc_stencil2d(int type, int ry, int rx, const void *w, int boundary, const void *cval, const void *in, int64_t ih,
                   int64_t iw, void *out, int64_t h, int64_t wd, int accumulate, int nth) {

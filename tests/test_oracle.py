@@ -139,3 +139,72 @@ def test_f64_oracle_is_accurate(orc):
     xs = rng.standard_normal(1 << 20).astype(np.float32)
     exact = float(np.sum(xs.astype(np.float64)))  # pairwise in f64
     assert abs(float(orc.fold_f64("+", 0.0, xs)) - exact) <= 1e-9 * max(1.0, abs(exact))
+
+
+# ---- rank-3 stencils (planes outer, then rows, then columns)
+PAD_MODE = {0: "edge", 1: "reflect", 2: "wrap", 3: "constant"}  # clamp, mirror, wrap, constant
+
+
+def stencil3d_numpy(w, x, b, cval):
+    """The same weighted sum from numpy's padding modes: Accelerate's mirror
+    (i < 0 -> -i, i >= n -> 2n - i - 2) is numpy's 'reflect'."""
+    rz, ry, rx = (s // 2 for s in w.shape)
+    kw = {"constant_values": cval} if b == 3 else {}
+    p = np.pad(x, ((rz, rz), (ry, ry), (rx, rx)), mode=PAD_MODE[b], **kw)
+    d, h, wd = x.shape
+    out = np.zeros_like(x)
+    for dz in range(w.shape[0]):
+        for dy in range(w.shape[1]):
+            for dx in range(w.shape[2]):
+                out += w[dz, dy, dx] * p[dz:dz + d, dy:dy + h, dx:dx + wd]
+    return out
+
+
+@pytest.mark.parametrize("b", [0, 1, 2, 3])
+@pytest.mark.parametrize("dt", [np.int32, np.int64, np.float64])
+@pytest.mark.parametrize("pattern", [(3, 3, 3), (1, 3, 5), (5, 1, 3), (3, 5, 1)])
+def test_stencil3d_against_numpy(orc, b, dt, pattern):
+    # small integer values: every sum is exact, so any order must agree
+    rng = np.random.default_rng(sum(pattern) * 10 + b)
+    x = rng.integers(-50, 50, size=(6, 7, 9)).astype(dt)
+    w = rng.integers(-3, 4, size=pattern).astype(dt)
+    w.flat[0] = 0  # a tap outside the pattern
+    got = orc.stencil3d(w, x, boundary=b, cval=-11)
+    assert np.array_equal(got, stencil3d_numpy(w, x, b, dt(-11)))
+    assert np.array_equal(orc.stencil3d(w, x, boundary=b, cval=-11, nthreads=4), got)
+
+
+@pytest.mark.parametrize("b", [0, 1, 2, 3])
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_stencil3d_is_planes_of_2d_in_order(orc, b, dt):
+    # Float taps with fused multiply-adds: bit-exact against the rank-2 oracle
+    # run plane by plane (dz = -rz .. rz), each continuing the accumulator,
+    # which pins the planes-outer tap order.
+    rng = np.random.default_rng(b)
+    x = rng.random((5, 6, 7)).astype(dt)
+    w = rng.standard_normal((3, 3, 3)).astype(dt)
+    cval = dt(0.25)
+    got = orc.stencil3d(w, x, boundary=b, cval=cval)
+    d = x.shape[0]
+    for z in range(d):
+        acc = np.full(x.shape[1:], dt(-0.0))
+        for k, dz in enumerate((-1, 0, 1)):
+            zz = z + dz
+            if 0 <= zz < d:
+                plane = x[zz]
+            elif b == 3:
+                plane = np.full(x.shape[1:], cval)
+            else:
+                zz = {0: min(max(zz, 0), d - 1), 1: -zz if zz < 0 else 2 * d - zz - 2, 2: zz % d}[b]
+                plane = x[zz]
+            acc = orc.stencil2d(w[k], plane, boundary=b, cval=cval, accumulate_onto=acc)
+        assert np.array_equal(got[z], acc), z
+
+
+def test_stencil3d_flat_pattern_is_2d(orc):
+    rng = np.random.default_rng(7)
+    x = rng.random((4, 8, 9)).astype(np.float32)
+    w = rng.standard_normal((1, 3, 5)).astype(np.float32)
+    got = orc.stencil3d(w, x, boundary=1)
+    for z in range(4):
+        assert np.array_equal(got[z], orc.stencil2d(w[0], x[z], boundary=1))

@@ -84,6 +84,7 @@ SIGNATURES = {
     "acc_permute": ([_I, _I, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_permute_clone": ([_I, _I, _P, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_stencil2d": ([_I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _P], _I),
+    "acc_stencil3d": ([_I, _I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _L, _P], _I),
     "acc_stencil2d_pair": ([_I, _I, _I, _P, _P, _I, _P, _I, _P, _P, _L, _L, _P, _L, _L, _P, _P], _I),
     "acc_batch_create": ([_I, _P, _L, _P], _I),
     "acc_batch_capture": ([_P, _P], _I),
@@ -372,6 +373,31 @@ def stencil(weights: Sequence[Sequence[float]], xs: torch.Tensor, boundary="clam
     st = lib().acc_stencil2d(tc, ky // 2, kx // 2, ctypes.cast(warr, ctypes.c_void_p), b, cvp, _ptr(xs),
                              _ptr(out), h, w, _stream(stream))
     _check(st, "stencil")
+    return out
+
+
+def stencil3d(weights, xs: torch.Tensor, boundary="clamp", cval=None, stream=None) -> torch.Tensor:
+    """stencil over a rank-3 array [planes][rows][columns] with a weighted-sum
+    stencil function; weights is a (2rz+1) x (2ry+1) x (2rx+1) nested list
+    (planes outer, as the reference's rank-3 patterns)."""
+    xs = _dev(xs)
+    if xs.dim() != 3:
+        raise ValueError("stencil3d takes a rank-3 array")
+    tc = type_of(xs)
+    planes = [[list(r) for r in p] for p in weights]
+    kz, ky, kx = len(planes), len(planes[0]), len(planes[0][0])
+    if kz % 2 == 0 or ky % 2 == 0 or kx % 2 == 0 or any(len(p) != ky or any(len(r) != kx for r in p)
+                                                         for p in planes):
+        raise ValueError("stencil pattern must be odd-sized and rectangular")
+    flat = [v for p in planes for r in p for v in r]
+    warr = (_CTYPES[tc] * len(flat))(*flat)
+    out = torch.empty_like(xs)
+    b = BOUNDARIES[boundary] if isinstance(boundary, str) else boundary
+    cvp, keep = _seed_ptr(tc, cval if cval is not None else 0)
+    d, h, w = xs.shape
+    st = lib().acc_stencil3d(tc, kz // 2, ky // 2, kx // 2, ctypes.cast(warr, ctypes.c_void_p), b, cvp, _ptr(xs),
+                             _ptr(out), d, h, w, _stream(stream))
+    _check(st, "stencil3d")
     return out
 
 

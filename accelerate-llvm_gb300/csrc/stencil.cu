@@ -19,7 +19,7 @@
 // results are bit-identical to a sequential C evaluation with C99 fma()
 // (correctly rounded).  Taps whose weight is exactly zero are not part of the
 // pattern and are not read.
-#include "common.cuh"
+#include "stencil_common.cuh"
 
 namespace accgb {
 
@@ -43,28 +43,6 @@ struct StencilArgs {
   int tma;
   uint32_t *err;
 };
-
-__device__ __forceinline__ int64_t bound_index(int64_t i, int64_t n, int b) {
-  if (i < 0) {
-    if (b == ACC_CLAMP) i = 0;
-    else if (b == ACC_MIRROR) i = -i;
-    else if (b == ACC_WRAP) i = n + i;
-  } else if (i >= n) {
-    if (b == ACC_CLAMP) i = n - 1;
-    else if (b == ACC_MIRROR) i = n - (i - n + 2);
-    else if (b == ACC_WRAP) i = i - n;
-  }
-  // Radii larger than the extent: the reference's remap would step out of
-  // the array again; keep the read inside it.
-  return i < 0 ? 0 : (i >= n ? n - 1 : i);
-}
-
-// One tap: acc + w*x, fused (a single rounding) for floats, wrapping for ints.
-template <class T> __device__ __forceinline__ T fma_tap(T w, T x, T acc) {
-  if constexpr (std::is_same<T, float>::value) return __fmaf_rn(w, x, acc);
-  else if constexpr (std::is_same<T, double>::value) return __fma_rn(w, x, acc);
-  else { using U = typename IntBits<T>::U; return (T)((U)acc + (U)w * (U)x); }
-}
 
 // RM: the largest radius this instantiation handles (ry, rx <= RM); PX: the
 // halo width in x, RM rounded up to 16 bytes.

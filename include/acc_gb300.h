@@ -282,6 +282,19 @@ int acc_stencil2d_pair(int type, int ry, int rx, const void *wa_w,
                        int64_t ha, int64_t wa, const void *b, int64_t hb,
                        int64_t wb, void *out, void *stream);
 
+/* stencil over a rank-3 array in[d][h][w] with a weighted-sum stencil
+ * function of (2rz+1) x (2ry+1) x (2rx+1) taps:
+ *     out[z][y][x] = sum w[((dz+rz)*(2ry+1)+(dy+ry))*(2rx+1)+(dx+rx)] * in[z+dz][y+dy][x+dx]
+ * in that tap order (planes outer, then rows, then columns: a rank-3
+ * pattern is a tuple of rank-2 patterns over the outermost index,
+ * StencilRtup*, CodeGen/Stencil.hs:126-180); arithmetic, zero-weight taps,
+ * `boundary` (applied to every index component), `cval` and the types as
+ * for acc_stencil2d; rz, ry, rx in [0, 4].  `weights` is a HOST pointer.
+ * Replaces stencil1Op / stencilCore on DIM3 arrays (PTX/Execute.hs:652-748). */
+int acc_stencil3d(int type, int rz, int ry, int rx, const void *weights,
+                  int boundary, const void *cval, const void *in, void *out,
+                  int64_t d, int64_t h, int64_t w, void *stream);
+
 /* ---------------------------------------------------------------- batches */
 
 /* Many independent fold / scanl1 requests in ONE persistent kernel launch.

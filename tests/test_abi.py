@@ -70,3 +70,10 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 0, N, N, out, N, 1, 4, N, N) == 1  # missing inputs
     assert lib.acc_scan_zipwith(0, 4, 0, 0, 0, 0, out, out, out, N, 1, 4, N, N) == 2  # zipWith (.&.) unsupported
     assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 2, out, out, out, N, 1, 4, out, N) == 1  # scanl' without sums
+    # rank-3 stencils
+    assert lib.acc_stencil3d(3, 5, 1, 1, out, 0, N, out, out, 4, 4, 4, N) == 1  # radius above 4
+    assert lib.acc_stencil3d(3, 1, 1, 1, out, 3, N, out, out, 4, 4, 4, N) == 1  # constant without a value
+    assert lib.acc_stencil3d(3, 1, 1, 1, out, 9, N, out, out, 4, 4, 4, N) == 1  # bad boundary
+    assert lib.acc_stencil3d(2, 1, 1, 1, out, 0, N, out, out, 4, 4, 4, N) == 2  # Word32 unsupported
+    assert lib.acc_stencil3d(3, 1, 1, 1, N, 0, N, out, out, 4, 4, 4, N) == 1   # no weights
+    assert lib.acc_stencil3d(3, 1, 1, 1, N, 0, N, N, N, 0, 4, 4, N) == 0      # empty: nothing to do

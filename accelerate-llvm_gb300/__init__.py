@@ -77,6 +77,7 @@ SIGNATURES = {
     "acc_fold": ([_I, _I, _I, _P, _P, _L, _L, _P, _P], _I),
     "acc_fold_zipwith": ([_I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_fold_seg": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
+    "acc_fold_seg_zipwith": ([_I, _I, _I, _I, _P, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_fold_seg_lengths": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_scan": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_scan_noalloc": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
@@ -249,6 +250,28 @@ def _fold_seg(f, z, xs, seg, prec, stream, offsets):
     fn = lib().acc_fold_seg if offsets else lib().acc_fold_seg_lengths
     _check(fn(op_of(f), tc, PRECS[prec], _ptr(xs), _ptr(seg), st_, _ptr(out), outer, inner, nseg, sp,
               _stream(stream)), "foldSeg")
+    return out
+
+
+def fold_seg_zipwith(f, g, z, xs: torch.Tensor, ys: torch.Tensor, seg: torch.Tensor, prec=None, stream=None):
+    """foldSeg f z (zipWith g xs ys) seg with the zipWith fused into the
+    segmented fold (acc_fold_seg_zipwith); z = None gives fold1Seg; `seg`
+    holds nseg+1 offsets."""
+    xs, ys, seg = _dev(xs), _dev(ys), _dev(seg)
+    if xs.shape != ys.shape or xs.dtype != ys.dtype:
+        raise ValueError("zipWith of arrays of different shapes or types")
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1]
+    outer = 1
+    for d in shape[:-1]:
+        outer *= d
+    nseg = seg.numel() - 1
+    out = torch.empty(shape[:-1] + (nseg,), dtype=xs.dtype, device=xs.device)
+    sp, _keep = _seed_ptr(tc, z)
+    _check(lib().acc_fold_seg_zipwith(op_of(f), op_of(g), tc, PRECS[prec], _ptr(xs), _ptr(ys), _ptr(seg),
+                                      type_of(seg), _ptr(out), outer, inner, nseg, sp, _stream(stream)),
+           "foldSeg_zipwith")
     return out
 
 

@@ -103,6 +103,20 @@ template <class T> struct Prim<ACC_XOR, T> {
   __device__ __forceinline__ static T ap(T a, T b) { return a ^ b; }
 };
 
+// One element of a fused zipWith producer: g x y for the primitive g = zop,
+// in the element type (integers wrap; __fmul_rn / __fadd_rn keep each
+// product or sum rounded on its own, never contracted into the consumer's
+// accumulation).
+template <class T>
+__device__ __forceinline__ T zip_elem(int zop, T x, T y) {
+  switch (zop) {
+    case ACC_ADD: return Prim<ACC_ADD, T>::ap(x, y);
+    case ACC_MUL: return Prim<ACC_MUL, T>::ap(x, y);
+    case ACC_MIN: return Prim<ACC_MIN, T>::ap(x, y);
+    default: return Prim<ACC_MAX, T>::ap(x, y);
+  }
+}
+
 // ----------------------------------------------------------------- accumulators
 // An accumulator policy describes the running state S of a reduction over
 // elements of T: lift one element, combine two states (left operand first),

@@ -46,6 +46,8 @@ struct SegArgs {
   int64_t long_ctas;   // CTAs [0, long_ctas) work on the list
   int64_t long_cap;    // capacity of the list
   uint32_t *err;
+  const void *in2;     // ZIP kernels: the folded element i is zop(in[i], in2[i])
+  int zop;
 };
 
 __device__ __forceinline__ int64_t seg_off(const SegArgs &a, int64_t i) {
@@ -102,11 +104,55 @@ __device__ __forceinline__ typename A::S seg_span(const T *p, int64_t len, int64
   return acc;
 }
 
-template <int OP, class T, int PREC>
+// seg_span over the fused producer zipWith zop p q: the vector body when p
+// and q share their 16-byte alignment phase, a scalar stride otherwise.
+template <class A, class T>
+__device__ __forceinline__ typename A::S seg_span_zip(const T *p, const T *q, int zop, int64_t len, int64_t t,
+                                                      int64_t nt) {
+  using S = typename A::S;
+  constexpr int VEC = 16 / sizeof(T);
+  S acc = A::id();
+  const uintptr_t addr = reinterpret_cast<uintptr_t>(p);
+  if (((addr ^ reinterpret_cast<uintptr_t>(q)) & 15u) != 0u) {
+    for (int64_t i = t; i < len; i += nt) acc = A::push(acc, zip_elem(zop, ld_stream(p + i), ld_stream(q + i)));
+    return acc;
+  }
+  int64_t head = (int64_t)(((16u - (addr & 15u)) & 15u) / sizeof(T));
+  if (head > len) head = len;
+  if (t < head) acc = A::push(acc, zip_elem(zop, ld_stream(p + t), ld_stream(q + t)));
+  const int64_t nvec = (len - head) / VEC;
+  const uint4 *pv = reinterpret_cast<const uint4 *>(p + head);
+  const uint4 *qv = reinterpret_cast<const uint4 *>(q + head);
+  for (int64_t i = t; i < nvec; i += nt) {
+    const uint4 v = ld_stream16(pv + i), w = ld_stream16(qv + i);
+    T e[VEC], f[VEC];
+    memcpy(e, &v, 16);
+    memcpy(f, &w, 16);
+#pragma unroll
+    for (int k = 0; k < VEC; ++k) acc = A::push(acc, zip_elem(zop, e[k], f[k]));
+  }
+  const int64_t tail0 = head + nvec * VEC;
+  if (tail0 + t < len) acc = A::push(acc, zip_elem(zop, ld_stream(p + tail0 + t), ld_stream(q + tail0 + t)));
+  return acc;
+}
+
+// With ZIP the folded array is the fused producer zipWith zop in in2.
+template <int OP, class T, int PREC, bool ZIP = false>
 __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
   const T *in = static_cast<const T *>(a.in);
+  const T *in2 = static_cast<const T *>(a.in2);
+  (void)in2;
+  // Element i of row r, and the fold of a span of row r.
+  auto elem = [&](const T *row, const T *row2, int64_t i) -> T {
+    if constexpr (ZIP) return zip_elem(a.zop, row[i], row2[i]);
+    else { (void)row2; return row[i]; }
+  };
+  auto span = [&](const T *row, const T *row2, int64_t len, int64_t t, int64_t nt) -> S {
+    if constexpr (ZIP) return seg_span_zip<A, T>(row, row2, a.zop, len, t, nt);
+    else { (void)row2; return seg_span<A, T>(row, len, t, nt); }
+  };
   T *out = static_cast<T *>(a.out);
   const int lane = threadIdx.x & 31;
   __shared__ S s_part[8];
@@ -118,7 +164,7 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
     for (int64_t job = blockIdx.x; job < nl * a.outer; job += a.long_ctas) {
       const int64_t r = job / nl, s = a.longs[job % nl];
       const int64_t u = seg_off(a, s), v = seg_off(a, s + 1);
-      S acc = seg_span<A, T>(in + r * a.inner + u, v - u, threadIdx.x, blockDim.x);
+      S acc = span(in + r * a.inner + u, ZIP ? in2 + r * a.inner + u : nullptr, v - u, threadIdx.x, blockDim.x);
       acc = warp_reduce<A>(acc);
       if (lane == 0) s_part[threadIdx.x >> 5] = acc;
       __syncthreads();
@@ -141,6 +187,7 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
     const int64_t r = job / groups, g = job % groups;
     const int64_t s = g * 32 + lane;
     const T *row = in + r * a.inner;
+    const T *row2 = ZIP ? in2 + r * a.inner : nullptr;
     int64_t u = 0, v = 0;
     bool valid = s < a.nseg;
     if (valid) {
@@ -158,8 +205,8 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
         S acc;
         int64_t i = u;
         if (a.has_seed) acc = A::lift(from_bits<T>(a.seed));
-        else acc = A::lift(row[i++]);
-        for (; i < v; ++i) acc = A::push(acc, row[i]);
+        else acc = A::lift(elem(row, row2, i++));
+        for (; i < v; ++i) acc = A::push(acc, elem(row, row2, i));
         out[r * a.nseg + s] = A::lower(acc);
       }
     }
@@ -170,7 +217,7 @@ __global__ void __launch_bounds__(256) foldseg_main(SegArgs a) {
       med &= med - 1;
       const int64_t mu = __shfl_sync(0xffffffffu, u, src);
       const int64_t mv = __shfl_sync(0xffffffffu, v, src);
-      S acc = seg_span<A, T>(row + mu, mv - mu, lane, 32);
+      S acc = span(row + mu, ZIP ? row2 + mu : nullptr, mv - mu, lane, 32);
       acc = warp_reduce<A>(acc);
       if (lane == 0) {
         if (a.has_seed) acc = A::comb(A::lift(from_bits<T>(a.seed)), acc);
@@ -692,9 +739,11 @@ int foldseg_tile_typed(Workspace *w, const T *in, const void *off, int off64, T 
 }
 
 // ----------------------------------------------------------------- host side
-template <int OP, class T, int PREC>
+// The per-segment path; with ZIP over the fused producer zipWith zop in in2.
+template <int OP, class T, int PREC, bool ZIP = false>
 int foldseg_typed(Workspace *w, const T *in, const void *off, int off64, T *out, int64_t outer,
-                  int64_t inner, int64_t nseg, bool has_seed, uint64_t seed, cudaStream_t s) {
+                  int64_t inner, int64_t nseg, bool has_seed, uint64_t seed, cudaStream_t s,
+                  const T *in2 = nullptr, int zop = 0) {
   const Device &d = device_info();
   // Scratch: the list of long segments (at most inner / LONG_SEG of them).
   int64_t maxlong = inner / LONG_SEG + 1;
@@ -709,6 +758,8 @@ int foldseg_typed(Workspace *w, const T *in, const void *off, int off64, T *out,
   a.longs = static_cast<int64_t *>(w->scratch);
   a.long_cap = maxlong;
   a.err = w->words + W_ERR;
+  a.in2 = in2;
+  a.zop = zop;
   // Only a row longer than LONG_SEG can hold a long segment.
   a.long_ctas = 0;
   if (inner > LONG_SEG) {
@@ -725,7 +776,7 @@ int foldseg_typed(Workspace *w, const T *in, const void *off, int off64, T *out,
   int64_t sb = cdiv_h(groups, 8);
   if (sb > (int64_t)d.sms * 64) sb = (int64_t)d.sms * 64;
   if (sb < 1) sb = 1;
-  foldseg_main<OP, T, PREC><<<(unsigned)(a.long_ctas + sb), 256, 0, s>>>(a);
+  foldseg_main<OP, T, PREC, ZIP><<<(unsigned)(a.long_ctas + sb), 256, 0, s>>>(a);
   return check_launch();
 }
 
@@ -809,4 +860,44 @@ extern "C" int acc_fold_seg_lengths(int op, int type, int prec, const void *in, 
   st = scan_offsets(w, length_type, lengths, offsets, nseg, s);
   if (st) return st;
   return foldseg_dispatch(w, op, type, prec, in, offsets, length_type == ACC_I64, out, outer, inner, nseg, seed, s);
+}
+
+// foldSeg f z (zipWith g xs ys): the reference fuses the producer into the
+// segmented fold's kernel (its delayed input, PTX/CodeGen/FoldSeg.hs:56-458
+// reading a MIRDelayed array).  Here the per-segment kernels read both arrays
+// and zip each element as they load it (the zipped array is never written).
+// f in {+, min, max}, g in {+, *, min, max}, Int32 / Int64 / Float32 /
+// Float64, as for the fused fold and scans.
+extern "C" int acc_fold_seg_zipwith(int op, int zop, int type, int prec, const void *xs, const void *ys,
+                                    const void *offsets, int offset_type, void *out, int64_t outer, int64_t inner,
+                                    int64_t nseg, const void *seed, void *stream) {
+  int st = fold_seg_check(type, offset_type, xs, offsets, out, outer, inner, nseg);
+  if (st) return st;
+  if (op < ACC_ADD || op > ACC_XOR || zop < ACC_ADD || zop > ACC_XOR) return ACC_ERR_INVALID;
+  if (outer > 0 && inner > 0 && nseg > 0 && !ys) return ACC_ERR_INVALID;
+  if (op != ACC_ADD && op != ACC_MIN && op != ACC_MAX) return ACC_ERR_UNSUPPORTED;
+  if (zop != ACC_ADD && zop != ACC_MUL && zop != ACC_MIN && zop != ACC_MAX) return ACC_ERR_UNSUPPORTED;
+  if (type == ACC_U32) return ACC_ERR_UNSUPPORTED;
+  if (outer == 0 || nseg == 0) return ACC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Workspace *w = workspace(s, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  return with_type(type, [&](auto tv) -> int {
+    using T = decltype(tv);
+    const uint64_t sb = seed_bits<T>(seed);
+    return with_op<T>(op, [&](auto opc) -> int {
+      constexpr int OP = decltype(opc)::value;
+      if constexpr ((OP != ACC_ADD && OP != ACC_MIN && OP != ACC_MAX) || std::is_same<T, uint32_t>::value) {
+        return ACC_ERR_UNSUPPORTED;
+      } else {
+        return with_prec<OP, T>(prec, [&](auto pc) -> int {
+          constexpr int P = decltype(pc)::value;
+          return foldseg_typed<OP, T, P, true>(w, static_cast<const T *>(xs), offsets, offset_type == ACC_I64,
+                                               static_cast<T *>(out), outer, inner, nseg, seed != nullptr, sb, s,
+                                               static_cast<const T *>(ys), zop);
+        });
+      }
+    });
+  });
 }

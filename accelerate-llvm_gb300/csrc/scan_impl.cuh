@@ -66,19 +66,6 @@ struct ScanArgs {
   int zop;
 };
 
-// One element of a fused zipWith producer: g x y for the primitive g, in the
-// element type (integers wrap; __fmul_rn / __fadd_rn keep each product or
-// sum rounded on its own, never contracted into the scan's accumulation).
-template <class T>
-__device__ __forceinline__ T zip_elem(int zop, T x, T y) {
-  switch (zop) {
-    case ACC_ADD: return Prim<ACC_ADD, T>::ap(x, y);
-    case ACC_MUL: return Prim<ACC_MUL, T>::ap(x, y);
-    case ACC_MIN: return Prim<ACC_MIN, T>::ap(x, y);
-    default: return Prim<ACC_MAX, T>::ap(x, y);
-  }
-}
-
 __device__ __forceinline__ int swz(int row, int chunk) { return row * SCAN_ROW_BYTES + ((chunk ^ (row & 7)) << 4); }
 
 // Publish a look-back status of tile t: (flag, value), flag 1 = aggregate,

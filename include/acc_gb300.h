@@ -181,6 +181,19 @@ int acc_fold_seg_lengths(int op, int type, int prec, const void *in,
                          int64_t outer, int64_t inner, int64_t nseg,
                          const void *seed, void *stream);
 
+/* foldSeg f z (zipWith g xs ys) / fold1Seg f (zipWith g xs ys): a segmented
+ * fold whose input is the fused producer of two arrays.  Replaces foldSegOp
+ * on a delayed zipWith input (PTX/CodeGen/FoldSeg.hs:56-458, the MIRDelayed
+ * argument): the zipped array is never written.  xs, ys: outer*inner
+ * elements each, same layout; every zipped element is g x y rounded to
+ * `type`; offsets, out, seed and empty segments as for acc_fold_seg.
+ * op in {ADD, MIN, MAX}, zop in {ADD, MUL, MIN, MAX}, type in {I32, I64,
+ * F32, F64}; other combinations give ACC_ERR_UNSUPPORTED. */
+int acc_fold_seg_zipwith(int op, int zop, int type, int prec, const void *xs,
+                         const void *ys, const void *offsets, int offset_type,
+                         void *out, int64_t outer, int64_t inner, int64_t nseg,
+                         const void *seed, void *stream);
+
 /* ---------------------------------------------------------------- scan */
 
 /* scanl / scanl1 / scanr / scanr1 / scanl' / scanr' along the innermost

@@ -70,6 +70,12 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 0, N, N, out, N, 1, 4, N, N) == 1  # missing inputs
     assert lib.acc_scan_zipwith(0, 4, 0, 0, 0, 0, out, out, out, N, 1, 4, N, N) == 2  # zipWith (.&.) unsupported
     assert lib.acc_scan_zipwith(0, 1, 0, 0, 0, 2, out, out, out, N, 1, 4, out, N) == 1  # scanl' without sums
+    assert lib.acc_fold_seg_zipwith(0, 9, 0, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 1  # bad zip primitive
+    assert lib.acc_fold_seg_zipwith(0, 1, 0, 0, out, out, out, 3, out, 1, 4, 2, N, N) == 1  # bad offset type
+    assert lib.acc_fold_seg_zipwith(0, 1, 0, 0, out, N, out, 0, out, 1, 4, 2, N, N) == 1    # missing ys
+    assert lib.acc_fold_seg_zipwith(1, 1, 0, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 2  # fold op (*) unsupported
+    assert lib.acc_fold_seg_zipwith(0, 5, 0, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 2  # zipWith (.|.) unsupported
+    assert lib.acc_fold_seg_zipwith(0, 1, 2, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 2  # Word32 unsupported
     # rank-3 stencils
     assert lib.acc_stencil3d(3, 5, 1, 1, out, 0, N, out, out, 4, 4, 4, N) == 1  # radius above 4
     assert lib.acc_stencil3d(3, 1, 1, 1, out, 3, N, out, out, 4, 4, 4, N) == 1  # constant without a value

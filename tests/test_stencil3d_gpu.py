@@ -4,20 +4,14 @@ component remapped by the boundary: accelerate-llvm/.../CodeGen/
 Stencil.hs:126-253; PTX/Execute.hs:652-748).
 
 The rank-3 kernel has not yet been run on a GPU: these tests run only with
-ACC_GB300_TEST_STENCIL3D=1, so that the default GPU suite holds only checked
-kernels."""
-import os
-
+ACC_GB300_TEST_NEW_KERNELS=1 (helpers.not_yet_on_gpu)."""
 import numpy as np
 import pytest
 import torch
 
-from helpers import _diff, case_rng
+from helpers import _diff, case_rng, not_yet_on_gpu
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("ACC_GB300_TEST_STENCIL3D") != "1",
-                                 reason="rank-3 stencil kernel not yet checked on a GPU "
-                                        "(set ACC_GB300_TEST_STENCIL3D=1)")]
+pytestmark = [pytest.mark.gpu, not_yet_on_gpu]
 
 STYPES = {"f32": np.float32, "f64": np.float64, "i32": np.int32, "i64": np.int64}
 PATTERNS = [(3, 3, 3), (1, 3, 5), (5, 1, 3), (3, 5, 1), (9, 9, 9), (1, 1, 3)]

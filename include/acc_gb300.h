@@ -312,8 +312,8 @@ int acc_stencil3d(int type, int rz, int ry, int rx, const void *weights,
 
 /* Many independent fold / scanl1 requests in ONE persistent kernel launch.
  * No counterpart in the reference, which launches every skeleton separately
- * (PTX/Execute.hs:835-881); this is the batched execution the benchmark spec
- * asks for.  A request is fold z xs / fold1 xs (one output element) or
+ * (PTX/Execute.hs:835-881): batching amortises the launch and scheduling
+ * cost of many small arrays.  A request is fold z xs / fold1 xs (one output element) or
  * scanl1 xs (n outputs; with a seed, the seed is combined on the left of
  * every prefix) over one contiguous vector, element type ACC_I32 / ACC_I64 /
  * ACC_F32 / ACC_F64; every request of a batch uses the same primitive, one

@@ -83,3 +83,23 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_stencil3d(2, 1, 1, 1, out, 0, N, out, out, 4, 4, 4, N) == 2  # Word32 unsupported
     assert lib.acc_stencil3d(3, 1, 1, 1, N, 0, N, out, out, 4, 4, 4, N) == 1   # no weights
     assert lib.acc_stencil3d(3, 1, 1, 1, N, 0, N, N, N, 0, 4, 4, N) == 0      # empty: nothing to do
+
+
+def test_c_caller_links_and_validates(lib, tmp_path):
+    """The header compiles as strict C99 and a C program linked against the
+    library by name gets the same answers as the ctypes calls above (a
+    Haskell cbits binding is such a C caller)."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc") or shutil.which("cc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    libdir = ROOT / "accelerate-llvm_gb300"
+    exe = tmp_path / "abi_from_c"
+    cmd = [gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", f"-I{ROOT / 'include'}",
+           str(ROOT / "tests" / "abi_from_c.c"), f"-L{libdir}", "-laccgb", f"-Wl,-rpath,{libdir}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.strip().endswith("0 failed")

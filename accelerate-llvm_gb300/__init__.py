@@ -15,8 +15,9 @@ only); results are allocated here, as the reference allocates them with
 ``'+' '*' 'min' 'max' 'and' 'or' 'xor'``; anything else raises, as the
 reference's shim raises ``internalError "unsupported combine function"``.
 
-There is no CPU fallback: importing this module on a machine where the
-library cannot be loaded raises.
+There is no CPU fallback: the library is loaded on first use, and that first
+call raises on a machine where it cannot be loaded; host (CPU) tensors are
+refused with ValueError, never computed on the host.
 """
 from __future__ import annotations
 

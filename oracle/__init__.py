@@ -29,7 +29,7 @@ CODE_OF = {np.dtype(np.int32): I32, np.dtype(np.int64): I64, np.dtype(np.uint32)
            np.dtype(np.float32): F32, np.dtype(np.float64): F64}
 OPS = {"+": 0, "*": 1, "min": 2, "max": 3, "and": 4, "or": 5, "xor": 6}
 
-CFLAGS = ["-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
+CFLAGS = ["-O3", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 
 def build(force: bool = False) -> pathlib.Path:

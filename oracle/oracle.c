@@ -489,27 +489,56 @@ static inline int64_t bound_ix(int64_t i, int64_t n, int b) {
   return i < 0 ? 0 : (i >= n ? n - 1 : i);
 }
 
+/* Rank 1/2, split as the native backend splits it (Native/CodeGen/Stencil.hs:
+ * 55-140): outputs whose whole pattern lies inside the input take the
+ * `stencil_inside` path, which reads without boundary checks (here tap by tap
+ * over a row of outputs, so the compiler can vectorise across outputs); the
+ * rest take the `stencil_border` path, which remaps every access.  Both visit
+ * the non-zero taps of each output in the same order (rows outer, -r..r), so
+ * the split does not change a single result bit. */
 #define DEFINE_STENCIL(NAME, T, U, TAP, ID)                                                              \
   static void NAME##_stencil(int ry, int rx, const T *w, int b, const T *cval, const T *in, int64_t ih,        \
                              int64_t iw, T *out, int64_t h, int64_t wd, int accumulate, int nth) {       \
     const int64_t ip = iw, op = wd;                                                                          \
-    _Pragma("omp parallel for schedule(static) if (nth > 1)")                                                \
-    for (int64_t y = 0; y < h; ++y)                                                                          \
-      for (int64_t x = 0; x < wd; ++x) {                                                                     \
-        T acc = accumulate ? out[y * op + x] : (ID);                                                         \
-        for (int dy = -ry; dy <= ry; ++dy)                                                                   \
-          for (int dx = -rx; dx <= rx; ++dx) {                                                               \
-            const T wk = w[(dy + ry) * (2 * rx + 1) + (dx + rx)];                                            \
-            if (wk == 0) continue;                                                                           \
-            const int64_t yy = y + dy, xx = x + dx;                                                          \
-            T v;                                                                                             \
-            if (yy >= 0 && yy < ih && xx >= 0 && xx < iw) v = in[yy * ip + xx];                              \
-            else if (b == 3) v = *cval;                                                                      \
-            else v = in[bound_ix(yy, ih, b) * ip + bound_ix(xx, iw, b)];                                     \
-            acc = TAP(wk, v, acc);                                                                           \
-          }                                                                                                  \
-        out[y * op + x] = acc;                                                                               \
+    int ntap = 0, tdy[81], tdx[81];                                                                          \
+    T tw[81];                                                                                                \
+    for (int dy = -ry; dy <= ry; ++dy)                                                                       \
+      for (int dx = -rx; dx <= rx; ++dx) {                                                                   \
+        const T wk = w[(dy + ry) * (2 * rx + 1) + (dx + rx)];                                                \
+        if (wk == 0) continue;                                                                               \
+        tdy[ntap] = dy; tdx[ntap] = dx; tw[ntap] = wk; ++ntap;                                               \
       }                                                                                                      \
+    /* the inside region: [ry, ih-ry) x [rx, iw-rx), clipped to the output */                               \
+    const int64_t y0 = ry, y1 = ih - ry < h ? ih - ry : h;                                                   \
+    const int64_t x0 = rx, x1 = iw - rx < wd ? iw - rx : wd;                                                 \
+    _Pragma("omp parallel for schedule(static) if (nth > 1)")                                                \
+    for (int64_t y = 0; y < h; ++y) {                                                                        \
+      T *o = out + y * op;                                                                                   \
+      const int inside = y >= y0 && y < y1 && x0 < x1;                                                       \
+      const int64_t xa = inside ? x0 : wd, xb = inside ? x1 : wd;                                            \
+      if (inside) {                                                                                          \
+        if (!accumulate)                                                                                     \
+          for (int64_t x = xa; x < xb; ++x) o[x] = (ID);                                                     \
+        for (int k = 0; k < ntap; ++k) {                                                                     \
+          const T wk = tw[k];                                                                                \
+          const T *src = in + (y + tdy[k]) * ip + tdx[k];                                                    \
+          for (int64_t x = xa; x < xb; ++x) o[x] = TAP(wk, src[x], o[x]);                                    \
+        }                                                                                                    \
+      }                                                                                                      \
+      for (int64_t x = 0; x < wd; ++x) {                                                                     \
+        if (x == xa) { x = xb - 1; continue; }                                                               \
+        T acc = accumulate ? o[x] : (ID);                                                                    \
+        for (int k = 0; k < ntap; ++k) {                                                                     \
+          const int64_t yy = y + tdy[k], xx = x + tdx[k];                                                    \
+          T v;                                                                                               \
+          if (yy >= 0 && yy < ih && xx >= 0 && xx < iw) v = in[yy * ip + xx];                                \
+          else if (b == 3) v = *cval;                                                                        \
+          else v = in[bound_ix(yy, ih, b) * ip + bound_ix(xx, iw, b)];                                       \
+          acc = TAP(tw[k], v, acc);                                                                          \
+        }                                                                                                    \
+        o[x] = acc;                                                                                          \
+      }                                                                                                      \
+    }                                                                                                        \
   }
 /* One tap, acc + w*x: C99 fma (one rounding) for floats, wrapping for ints. */
 #define T_F32(w, x, acc) fmaf((w), (x), (acc))

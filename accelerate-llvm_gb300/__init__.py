@@ -165,6 +165,23 @@ def _dev(t: torch.Tensor) -> torch.Tensor:
     return t.contiguous()
 
 
+def _given(t, need: int, what: str, dtype=None):
+    """A caller-provided array that the library reads or writes in place (a
+    batch or serving request): the library sees only its address, so it must
+    be a contiguous CUDA tensor holding at least `need` elements, of `dtype`
+    when one is given.  Checked here because a short or host-side buffer would
+    otherwise be accessed out of bounds on the device."""
+    if not getattr(t, "is_cuda", False):
+        raise ValueError(f"{what}: arrays must be CUDA tensors")
+    if not t.is_contiguous():
+        raise ValueError(f"{what}: arrays must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{what}: element type {t.dtype}, expected {dtype}")
+    if t.numel() < need:
+        raise ValueError(f"{what}: {t.numel()} elements, at least {need} needed")
+    return t
+
+
 def sync(stream=None) -> None:
     """Wait for the stream and raise any device-side error (acc_sync)."""
     _check(lib().acc_sync(_stream(stream)), "acc_sync")
@@ -480,8 +497,11 @@ class Batch:
         self._keep = []
         arr = (Request * max(1, len(requests)))()
         for i, (kind, xs, out, seed) in enumerate(requests):
+            if kind not in ("fold", "scan"):
+                raise ValueError(f"batch request {i}: kind {kind!r}, expected 'fold' or 'scan'")
             xs = _dev(xs)
             tc = type_of(xs)
+            _given(out, 1 if kind == "fold" else xs.numel(), f"batch request {i} output", xs.dtype)
             self._keep += [xs, out]
             arr[i].kind = REQ_FOLD if kind == "fold" else REQ_SCAN
             arr[i].type = tc
@@ -550,6 +570,19 @@ def serve(requests, budget_bytes: int, slots: int = 8, mode: str = "batching"):
     arr = (ServeReq * max(1, len(requests)))()
     keep = []
     for i, (sk, xs, aux, out, n, m, t) in enumerate(requests):
+        if sk not in SKELETONS:
+            raise ValueError(f"request {i}: skeleton {sk!r}, expected one of {sorted(SKELETONS)}")
+        if n < 0 or m < 0:
+            raise ValueError(f"request {i}: negative extent")
+        what = f"request {i} ({sk})"
+        if sk == "permute":
+            _given(xs, n, what + " indices", torch.int32)
+            _given(out, m, what + " bins", torch.int32)
+        else:
+            _given(xs, n * m if sk == "stencil" else n, what + " input")
+            _given(out, {"fold": 1, "scan": n, "foldseg": m, "stencil": n * m}[sk], what + " output", xs.dtype)
+        if sk == "foldseg":
+            _given(aux, m + 1, what + " offsets", torch.int32)
         keep += [xs, aux, out]
         arr[i].skeleton = SKELETONS[sk]
         arr[i].type = type_of(xs) if sk != "permute" else I32

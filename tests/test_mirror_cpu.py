@@ -3,7 +3,8 @@ has no CPU fallback.  Every skeleton refuses host tensors with ValueError
 before any library call, so nothing is ever computed on the host; combine
 functions outside the fixed primitives and unsupported element types are
 refused as the reference's shim refuses them (`internalError "unsupported
-combine function"`)."""
+combine function"`); the buffers a caller hands to a batch or a serving run
+are checked for place, layout, type and size before the device sees them."""
 import numpy as np
 import pytest
 import torch
@@ -93,3 +94,44 @@ def test_seed_is_passed_as_one_host_element(mirror):
         assert got == value and keep is not None
     assert mirror._seed_ptr(mirror.I32, None) == (None, None)
     assert np.float32(mirror._CTYPES[mirror.F32](0.1).value) == np.float32(0.1)
+
+
+def test_batch_and_serve_refuse_host_tensors(mirror):
+    x, out = host(torch.int32, (16,)), host(torch.int32, (1,))
+    with pytest.raises(ValueError, match="CUDA tensors"):
+        mirror.Batch("+", [("fold", x, out, None)])
+    with pytest.raises(ValueError, match="CUDA tensors"):
+        mirror.serve([("fold", x, None, out, 16, 0, 0.0)], 1 << 20)
+    with pytest.raises(ValueError, match="kind"):
+        mirror.Batch("+", [("scanr", x, out, None)])
+    with pytest.raises(ValueError, match="skeleton"):
+        mirror.serve([("map", x, None, out, 16, 0, 0.0)], 1 << 20)
+
+
+class DeviceStub:
+    """Stands in for a device tensor: the checks of caller-provided batch and
+    serving buffers read only these attributes."""
+
+    def __init__(self, numel, dtype=torch.float32, contiguous=True):
+        self.is_cuda, self.dtype, self._n, self._c = True, dtype, numel, contiguous
+
+    def numel(self):
+        return self._n
+
+    def is_contiguous(self):
+        return self._c
+
+
+def test_caller_buffers_are_checked_before_the_device_sees_them(mirror):
+    # the library sees only an address: a short, mistyped or strided buffer
+    # would be read or written out of bounds on the device
+    g = mirror._given
+    assert g(DeviceStub(10), 10, "out", torch.float32).numel() == 10
+    with pytest.raises(ValueError, match="at least 11"):
+        g(DeviceStub(10), 11, "out")
+    with pytest.raises(TypeError, match="element type"):
+        g(DeviceStub(10, torch.int32), 1, "out", torch.float32)
+    with pytest.raises(ValueError, match="contiguous"):
+        g(DeviceStub(10, contiguous=False), 1, "out")
+    with pytest.raises(ValueError, match="CUDA tensors"):
+        g(torch.zeros(10), 1, "out")

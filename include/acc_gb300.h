@@ -128,7 +128,9 @@ const char *acc_strerror(int status);
  * reference's `get`/`block` on a Future (PTX/Execute/Async.hs:132-165). */
 int acc_sync(void *stream);
 
-/* Drop the cached temporaries of every stream (they are re-made on demand). */
+/* Drop the cached temporaries of every stream (they are re-made on demand).
+ * Waits for the device first; call it only while no other host thread is
+ * inside a library call, since those calls hold pointers into the cache. */
 int acc_release_workspaces(void);
 
 /* ---------------------------------------------------------------- fold */

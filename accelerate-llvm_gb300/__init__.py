@@ -580,6 +580,8 @@ def serve(requests, budget_bytes: int, slots: int = 8, mode: str = "batching"):
             _given(out, m, what + " bins", torch.int32)
         else:
             _given(xs, n * m if sk == "stencil" else n, what + " input")
+            if sk == "stencil" and xs.dtype not in (torch.float32, torch.float64):
+                raise TypeError(f"{what}: the 5-point stencil takes Float32 / Float64 grids")
             _given(out, {"fold": 1, "scan": n, "foldseg": m, "stencil": n * m}[sk], what + " output", xs.dtype)
         if sk == "foldseg":
             _given(aux, m + 1, what + " offsets", torch.int32)

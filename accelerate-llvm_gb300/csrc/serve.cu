@@ -113,6 +113,9 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
   for (int64_t i = 0; i < count; ++i) {
     const acc_serve_req &q = reqs[i];
     if (q.skeleton < ACC_SK_FOLD || q.skeleton > ACC_SK_STENCIL || q.n < 0 || q.m < 0) return ACC_ERR_INVALID;
+    if (q.type < ACC_I32 || q.type > ACC_F64) return ACC_ERR_INVALID;
+    // The 5-point weights (0.25, -1) are real numbers: Float32 / Float64 grids only.
+    if (q.skeleton == ACC_SK_STENCIL && q.type != ACC_F32 && q.type != ACC_F64) return ACC_ERR_UNSUPPORTED;
     if (i > 0 && q.arrival < reqs[i - 1].arrival) return ACC_ERR_INVALID;  // arrival order
     if (held_bytes(q) > budget_bytes) return ACC_ERR_TOO_LARGE;
     latency[i] = -1.0;

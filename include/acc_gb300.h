@@ -375,7 +375,8 @@ int acc_batch_load_tuning(const char *table_path);
  *   ACC_SK_SCAN     out = scanl1 (+) in[0..n)
  *   ACC_SK_FOLDSEG  out[0..m) = foldSeg (+) 0 in[0..n) with Int32 offsets aux[0..m]
  *   ACC_SK_PERMUTE  out[0..m) = histogram of the Int32 indices in[0..n) (permute (+) zeros idx 1)
- *   ACC_SK_STENCIL  out = 5-point stencil (0.25 N/S/E/W, -1 centre, clamp) of the n x m grid in */
+ *   ACC_SK_STENCIL  out = 5-point stencil (0.25 N/S/E/W, -1 centre, clamp) of the n x m grid in
+ *                   (Float32 / Float64 only; other types give ACC_ERR_UNSUPPORTED) */
 typedef enum acc_skeleton {
   ACC_SK_FOLD = 0,
   ACC_SK_SCAN = 1,

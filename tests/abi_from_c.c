@@ -89,6 +89,12 @@ int main(void) {
   memset(&sreq, 0, sizeof(sreq));
   expect("serve, no slots", acc_serve_run(&sreq, 1, one << 20, 0, 0, latency, NULL), ACC_ERR_INVALID);
   expect("serve, bad mode", acc_serve_run(&sreq, 1, one << 20, 4, 7, latency, NULL), ACC_ERR_INVALID);
+  sreq.type = 9;
+  expect("serve, bad element type", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL), ACC_ERR_INVALID);
+  sreq.skeleton = ACC_SK_STENCIL;
+  sreq.type = ACC_I32;
+  expect("serve, Int32 5-point stencil", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL),
+         ACC_ERR_UNSUPPORTED);
 
   printf("%d failed\n", failures);
   return failures;

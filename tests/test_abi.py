@@ -83,6 +83,13 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_stencil3d(2, 1, 1, 1, out, 0, N, out, out, 4, 4, 4, N) == 2  # Word32 unsupported
     assert lib.acc_stencil3d(3, 1, 1, 1, N, 0, N, out, out, 4, 4, 4, N) == 1   # no weights
     assert lib.acc_stencil3d(3, 1, 1, 1, N, 0, N, N, N, 0, 4, 4, N) == 0      # empty: nothing to do
+    # serving requests, checked before the device is touched
+    pkg = __import__("__graft_entry__").load_package()
+    req = pkg.ServeReq(skeleton=pkg.SK_STENCIL, type=0, n=4, m=4)  # an Int32 grid
+    lat = (ctypes.c_double * 1)()
+    assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 2   # 5-point weights need floats
+    req.type = 9
+    assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # bad element type
 
 
 def test_c_caller_links_and_validates(lib, tmp_path):

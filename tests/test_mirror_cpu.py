@@ -135,3 +135,9 @@ def test_caller_buffers_are_checked_before_the_device_sees_them(mirror):
         g(DeviceStub(10, contiguous=False), 1, "out")
     with pytest.raises(ValueError, match="CUDA tensors"):
         g(torch.zeros(10), 1, "out")
+
+
+def test_serve_stencil_takes_float_grids(mirror):
+    grid, out = DeviceStub(16, torch.int32), DeviceStub(16, torch.int32)
+    with pytest.raises(TypeError, match="Float32 / Float64"):
+        mirror.serve([("stencil", grid, None, out, 4, 4, 0.0)], 1 << 20)

@@ -403,6 +403,7 @@ static int batch_make(int op, const acc_request *reqs, int64_t count, const int3
     if (q.kind != ACC_REQ_FOLD && q.kind != ACC_REQ_SCAN) return ACC_ERR_INVALID;
     if (q.type != ACC_I32 && q.type != ACC_I64 && q.type != ACC_F32 && q.type != ACC_F64) return ACC_ERR_UNSUPPORTED;
     if (q.n < 0 || (q.n > 0 && (!q.in || !q.out))) return ACC_ERR_INVALID;
+    if (q.kind == ACC_REQ_FOLD && !q.out) return ACC_ERR_INVALID;  // fold z [] still writes z
     if (q.kind == ACC_REQ_FOLD && q.n == 0 && !q.has_seed) return ACC_ERR_EMPTY;
     const int ipt = norm_ipt(ipt_override ? ipt_override[i] : tuned_ipt(q.kind, q.type, q.n), q.type);
     const int64_t ts = (int64_t)ipt * BT;

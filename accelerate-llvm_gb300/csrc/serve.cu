@@ -116,6 +116,15 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
     if (q.type < ACC_I32 || q.type > ACC_F64) return ACC_ERR_INVALID;
     // The 5-point weights (0.25, -1) are real numbers: Float32 / Float64 grids only.
     if (q.skeleton == ACC_SK_STENCIL && q.type != ACC_F32 && q.type != ACC_F64) return ACC_ERR_UNSUPPORTED;
+    // Every buffer the request reads or writes must be given: a null address
+    // would otherwise reach the device.
+    const int64_t nin = q.skeleton == ACC_SK_STENCIL ? q.n * q.m : q.n;
+    const int64_t nout = q.skeleton == ACC_SK_FOLD      ? 1
+                         : q.skeleton == ACC_SK_SCAN    ? q.n
+                         : q.skeleton == ACC_SK_STENCIL ? q.n * q.m
+                                                        : q.m;
+    if ((nin > 0 && !q.in) || (nout > 0 && !q.out) || (q.skeleton == ACC_SK_FOLDSEG && q.m > 0 && !q.aux))
+      return ACC_ERR_INVALID;
     if (i > 0 && q.arrival < reqs[i - 1].arrival) return ACC_ERR_INVALID;  // arrival order
     if (held_bytes(q) > budget_bytes) return ACC_ERR_TOO_LARGE;
     latency[i] = -1.0;

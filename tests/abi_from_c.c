@@ -83,12 +83,21 @@ int main(void) {
 
   /* batches and serving: the host-side checks that precede any device work */
   expect("batch create, no result pointer", acc_batch_create(ACC_ADD, &req, 1, NULL), ACC_ERR_INVALID);
+  req.kind = ACC_REQ_FOLD; /* fold z [] with nowhere to write z */
+  req.type = ACC_I32;
+  req.n = 0;
+  req.has_seed = 1;
+  expect("batch create, fold without output", acc_batch_create(ACC_ADD, &req, 1, &batch), ACC_ERR_INVALID);
   expect("batch launch, no batch", acc_batch_launch(NULL, NULL), ACC_ERR_INVALID);
   expect("batch destroy, no batch", acc_batch_destroy(batch), ACC_OK);
   expect("batch tuning, no path", acc_batch_load_tuning(NULL), ACC_ERR_INVALID);
   memset(&sreq, 0, sizeof(sreq));
   expect("serve, no slots", acc_serve_run(&sreq, 1, one << 20, 0, 0, latency, NULL), ACC_ERR_INVALID);
   expect("serve, bad mode", acc_serve_run(&sreq, 1, one << 20, 4, 7, latency, NULL), ACC_ERR_INVALID);
+  sreq.type = ACC_F32; /* a fold with no output buffer */
+  sreq.n = 16;
+  sreq.in = p;
+  expect("serve, fold without output", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL), ACC_ERR_INVALID);
   sreq.type = 9;
   expect("serve, bad element type", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL), ACC_ERR_INVALID);
   sreq.skeleton = ACC_SK_STENCIL;

@@ -90,6 +90,13 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 2   # 5-point weights need floats
     req.type = 9
     assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # bad element type
+    req = pkg.ServeReq(skeleton=pkg.SK_FOLDSEG, type=3, inp=16, out=16, n=64, m=4)
+    assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # foldSeg without offsets
+    req = pkg.ServeReq(skeleton=pkg.SK_SCAN, type=3, inp=16, n=64)
+    assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # scan without output
+    breq = pkg.Request(kind=pkg.REQ_FOLD, type=0, n=0, has_seed=1)                # fold z [] without output
+    h = ctypes.c_void_p()
+    assert lib.acc_batch_create(0, ctypes.byref(breq), 1, ctypes.byref(h)) == 1
 
 
 def test_c_caller_links_and_validates(lib, tmp_path):

@@ -507,6 +507,10 @@ extern "C" int acc_permute_clone(int op, int type, const void *defaults, const v
   if (m < 0 || (m > 0 && (!defaults || !out))) return ACC_ERR_INVALID;
   static const size_t esz[] = {4, 8, 4, 4, 8};
   if (type < ACC_I32 || type > ACC_F64) return ACC_ERR_INVALID;
+  // acc_permute's own argument checks, made before the clone so that a
+  // rejected call leaves `out` untouched.
+  if (n < 0 || (index_type != ACC_I32 && index_type != ACC_I64) || (!src && !cval) || (n > 0 && !idx))
+    return ACC_ERR_INVALID;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (m > 0) {
     cudaError_t e = cudaMemcpyAsync(out, defaults, (size_t)m * esz[type], cudaMemcpyDeviceToDevice, s);

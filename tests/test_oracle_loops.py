@@ -163,3 +163,87 @@ def test_permute_matches_loops(orc, dt, op):
         if j >= 0:
             ref[j] = f(xs[i], ref[j])  # new value first, old value second
     assert same(orc.permute(op, defaults, idx, xs), np.array(ref, dtype=dt))
+
+
+def loop_bound(i, n, b):
+    """Boundary remap of accelerate-llvm/.../CodeGen/Stencil.hs:224-253 (clamp,
+    mirror, wrap), kept inside the array when a radius exceeds the extent."""
+    if i < 0:
+        i = 0 if b == 0 else (-i if b == 1 else n + i)
+    elif i >= n:
+        i = n - 1 if b == 0 else (n - (i - n + 2) if b == 1 else i - n)
+    return min(max(i, 0), n - 1)
+
+
+def fma_exact(dt, w, v, acc):
+    """w*v + acc rounded once to dt (round to nearest, ties to even): the exact
+    value in rational arithmetic, then the nearest of the neighbouring values
+    of dt.  An exact zero takes the IEEE sign, which the double evaluation of
+    the same (then exact) expression gives."""
+    from fractions import Fraction
+    q = Fraction(float(w)) * Fraction(float(v)) + Fraction(float(acc))
+    if q == 0:
+        return dt(np.float64(w) * np.float64(v) + np.float64(acc))
+    if dt is np.float64:
+        return np.float64(float(q))  # int / int division: correctly rounded
+    c = np.float32(float(q))
+    near = [t for t in (np.nextafter(c, np.float32(-np.inf)), c, np.nextafter(c, np.float32(np.inf)))
+            if np.isfinite(t)]
+    return min(near, key=lambda t: (abs(Fraction(float(t)) - q), int(t.view(np.uint32)) & 1))
+
+
+def loop_stencil(w, x, b, cval, acc_from=None, out_shape=None):
+    """Weighted sum, taps rows outer and -r..r, one fused multiply-add per
+    non-zero tap (rounded once), integers wrapping."""
+    dt = x.dtype.type
+    ky, kx = w.shape
+    ry, rx = ky // 2, kx // 2
+    ih, iw = x.shape
+    h, wd = out_shape if out_shape is not None else x.shape
+    out = np.empty((h, wd), dtype=x.dtype)
+    f = prim("+", dt)
+    for y in range(h):
+        for xo in range(wd):
+            acc = acc_from[y, xo] if acc_from is not None else (dt(-0.0) if x.dtype.kind == "f" else dt(0))
+            for dy in range(-ry, ry + 1):
+                for dx in range(-rx, rx + 1):
+                    wk = w[dy + ry, dx + rx]
+                    if wk == 0:
+                        continue
+                    yy, xx = y + dy, xo + dx
+                    if 0 <= yy < ih and 0 <= xx < iw:
+                        v = x[yy, xx]
+                    elif b == 3:
+                        v = dt(cval)
+                    else:
+                        v = x[loop_bound(yy, ih, b), loop_bound(xx, iw, b)]
+                    if x.dtype.kind == "f":
+                        acc = fma_exact(dt, wk, v, acc)
+                    else:
+                        acc = f(acc, prim("*", dt)(wk, v))
+            out[y, xo] = acc
+    return out
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64, np.int32, np.int64])
+@pytest.mark.parametrize("b", [0, 1, 2, 3])
+def test_stencil_matches_loops(orc, dt, b):
+    rng = case_rng("loops_stencil", np.dtype(dt).name, b)
+    for (ky, kx), shape in [((3, 3), (6, 7)), ((1, 5), (4, 9)), ((5, 3), (7, 5)), ((3, 1), (2, 3)), ((5, 5), (3, 3))]:
+        if np.dtype(dt).kind == "f":
+            x = rng.random(shape).astype(dt)
+            w = rng.uniform(-1, 1, (ky, kx)).astype(dt)
+        else:
+            x = rng.integers(-1000, 1000, shape).astype(dt)
+            w = rng.integers(-3, 4, (ky, kx)).astype(dt)
+        w[rng.random(w.shape) < 0.2] = 0
+        got = orc.stencil2d(w, x, boundary=b, cval=dt(5))
+        assert same(got, loop_stencil(w, x, b, 5)), (ky, kx, shape)
+        # stencil2: a second input continues the accumulator over the
+        # intersection of the two extents
+        x2 = x[: shape[0] - 1, 1:] if shape[0] > 1 and shape[1] > 1 else x
+        out_shape = (min(x.shape[0], x2.shape[0]), min(x.shape[1], x2.shape[1]))
+        first = orc.stencil2d(w, x, boundary=b, cval=dt(5), out_shape=out_shape)
+        got = orc.stencil2d(w, x2, boundary=b, cval=dt(5), accumulate_onto=first, out_shape=out_shape)
+        ref = loop_stencil(w, x2, b, 5, acc_from=loop_stencil(w, x, b, 5, out_shape=out_shape), out_shape=out_shape)
+        assert same(got, ref), ("pair", ky, kx, shape)

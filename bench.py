@@ -283,7 +283,9 @@ def run_ours(args, rank, world):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
     }
-    if rank == 0 and not args.no_cpu:
+    # The CPU baseline is timed once, on rank 0 of a single-GPU run: with more
+    # replicas the other GPUs would sit idle while the host cores are busy.
+    if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(args.cpu_scale)
     return line
 

@@ -10,18 +10,10 @@ Comparison rules (the tolerances are written here, once):
     1.0, a sparse 0.5 / 2.0), whose products are exact in any order: a
     coverage check that every element is combined exactly once.
 """
-import os
 import zlib
 
 import numpy as np
 import pytest
-
-# Kernels written without a GPU at hand: their GPU tests run only with
-# ACC_GB300_TEST_NEW_KERNELS=1 until a GPU run has passed them, so that the
-# default GPU suite holds only kernels that have been checked on a GPU.
-not_yet_on_gpu = pytest.mark.skipif(os.environ.get("ACC_GB300_TEST_NEW_KERNELS") != "1",
-                                    reason="kernel not yet checked on a GPU (ACC_GB300_TEST_NEW_KERNELS=1 runs it)")
-
 
 def case_rng(*parts):
     """A generator seeded from the test case's parameters, the same in every

@@ -1,19 +1,16 @@
 """foldSeg f z (zipWith g xs ys) with the zipWith fused into the per-segment
 kernels (the reference's delayed foldSeg input, PTX/CodeGen/FoldSeg.hs:56-458)
 against the oracle: the zipped array is formed in the element type, then
-folded per segment by the oracle; comparison rules as for acc_fold_seg.
-
-The fused segmented fold has not yet been run on a GPU: these tests run only
-with ACC_GB300_TEST_NEW_KERNELS=1 (helpers.not_yet_on_gpu)."""
+folded per segment by the oracle; comparison rules as for acc_fold_seg."""
 import numpy as np
 import pytest
 import torch
 
-from helpers import TYPES, assert_fold_close, case_rng, gen, not_yet_on_gpu, seed_for
+from helpers import TYPES, assert_fold_close, case_rng, gen, seed_for
 from test_fold_zip_gpu import zipped
 from test_foldseg_gpu import segmentation
 
-pytestmark = [pytest.mark.gpu, not_yet_on_gpu]
+pytestmark = pytest.mark.gpu
 
 ZTYPES = ["i32", "i64", "f32", "f64"]
 FOLD_OPS = ["+", "min", "max"]

@@ -1,17 +1,14 @@
 """Rank-3 weighted-sum stencils on the GPU, bit-exact against the oracle's
 rank-3 restatement (planes outer, then rows, then columns; every index
 component remapped by the boundary: accelerate-llvm/.../CodeGen/
-Stencil.hs:126-253; PTX/Execute.hs:652-748).
-
-The rank-3 kernel has not yet been run on a GPU: these tests run only with
-ACC_GB300_TEST_NEW_KERNELS=1 (helpers.not_yet_on_gpu)."""
+Stencil.hs:126-253; PTX/Execute.hs:652-748)."""
 import numpy as np
 import pytest
 import torch
 
-from helpers import _diff, case_rng, not_yet_on_gpu
+from helpers import _diff, case_rng
 
-pytestmark = [pytest.mark.gpu, not_yet_on_gpu]
+pytestmark = pytest.mark.gpu
 
 STYPES = {"f32": np.float32, "f64": np.float64, "i32": np.int32, "i64": np.int64}
 PATTERNS = [(3, 3, 3), (1, 3, 5), (5, 1, 3), (3, 5, 1), (9, 9, 9), (1, 1, 3)]

@@ -511,6 +511,8 @@ extern "C" int acc_permute_clone(int op, int type, const void *defaults, const v
   // rejected call leaves `out` untouched.
   if (n < 0 || (index_type != ACC_I32 && index_type != ACC_I64) || (!src && !cval) || (n > 0 && !idx))
     return ACC_ERR_INVALID;
+  if (op < ACC_ADD || op > ACC_XOR) return ACC_ERR_INVALID;
+  if (op >= ACC_AND && (type == ACC_F32 || type == ACC_F64)) return ACC_ERR_UNSUPPORTED;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (m > 0) {
     cudaError_t e = cudaMemcpyAsync(out, defaults, (size_t)m * esz[type], cudaMemcpyDeviceToDevice, s);

@@ -72,16 +72,17 @@ extern "C" int acc_scan(int op, int type, int prec, int dir, int kind, const voi
 
 // --------------------------------------------------------------------------
 // acc_scan_noalloc: the same scan for callers that may not allocate device
-// memory.  A host that runs inside a CUDA stream capture, a real-time or
-// embedded integration with a fixed device-memory budget, or a plugin whose
-// process owns its own pool allocator cannot have this library call
-// cudaMalloc behind its back, which the per-stream workspace of acc_scan does
-// on first use and whenever an array needs more look-back slots.  This entry
-// point keeps its scratch (look-back status slots, tile ticket, error word)
-// in one file-scope device array instead, sized for NOALLOC_MAX_TILES tiles:
-// 2 MiB plus 256 bytes, held by every GPU that loads the library until the
-// process exits.  It therefore scans at most NOALLOC_MAX_ELEMS = 2^28
-// elements per row and rejects longer rows with ACC_ERR_TOO_LARGE.
+// memory.  An integration that runs under a fixed device-memory budget, a
+// plugin whose host process hands out all device memory from its own pool
+// allocator, or a latency-bound loop that must not stall on cudaMalloc (which
+// can synchronise the device) cannot have this library call cudaMalloc behind
+// its back, which the per-stream workspace of acc_scan does on first use and
+// whenever an array needs more look-back slots.  This entry point keeps its
+// scratch (look-back status slots, tile ticket, error word) in one
+// file-scope device array instead, sized for NOALLOC_MAX_TILES tiles: 2 MiB
+// plus 256 bytes, held by every GPU that loads the library until the process
+// exits.  It therefore scans at most NOALLOC_MAX_ELEMS = 2^28 elements per
+// row and rejects longer rows with ACC_ERR_TOO_LARGE.
 namespace accgb {
 
 constexpr int64_t NOALLOC_MAX_TILES = 1 << 17;
@@ -96,7 +97,6 @@ static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
 struct NoallocDevice {
   NoallocScratch *ptr = nullptr;  // device address of g_noalloc_scratch
-  uint32_t epoch = 0;
 };
 
 // Set-up, once per device, with that device current: the device address of
@@ -135,17 +135,16 @@ static int noalloc_scan_1d(NoallocDevice *nd, const T *in, T *out, T *total_out,
   const int64_t tile_elems = (int64_t)(tma ? SUB : 1) * SCAN_THREADS * ITEMS;
   const int64_t ntiles = cdiv_h(n, tile_elems);
   if (ntiles > NOALLOC_MAX_TILES) return ACC_ERR_TOO_LARGE;
-  // The array keeps the previous call's contents: the ticket and the error
-  // word must start at zero, and the status slots are tagged with a fresh
-  // epoch so that no slot of an earlier call can match.
+  // The array keeps the previous call's contents.  Before the launch, in
+  // stream order, the ticket and the error word are set to zero and so are
+  // the status slots of this call's tiles: a slot then holds a tag of this
+  // call (epoch 1) only once one of its tiles has published, whatever an
+  // earlier call left there.  The clearing is 16 bytes per tile of 16 to 64
+  // KiB, and no epoch is kept on the host, so no host state changes between
+  // calls.
   cudaError_t e = cudaMemsetAsync(nd->ptr->words, 0, sizeof(nd->ptr->words), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(nd->ptr->status, 0, (size_t)ntiles * 2 * sizeof(uint64_t), s);
   if (e != cudaSuccess) return cuda_status(e);
-  nd->epoch += 1;
-  if (nd->epoch >= (1u << 30)) {
-    e = cudaMemsetAsync(nd->ptr->status, 0, sizeof(nd->ptr->status), s);
-    if (e != cudaSuccess) return cuda_status(e);
-    nd->epoch = 1;
-  }
   ScanArgs a{};
   a.in = in; a.out = out; a.total_out = total_out; a.seed_out = seed_out;
   a.n = n;
@@ -155,7 +154,7 @@ static int noalloc_scan_1d(NoallocDevice *nd, const T *in, T *out, T *total_out,
   a.status = nd->ptr->status;
   a.ticket = nd->ptr->words + 1;
   a.err = nd->ptr->words + 0;
-  a.epoch = nd->epoch;
+  a.epoch = 1;
   a.has_seed = has_seed;
   a.exclusive = exclusive;
   a.tma_in = a.tma_out = tma;

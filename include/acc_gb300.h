@@ -226,14 +226,17 @@ int acc_scan_zipwith(int op, int zop, int type, int prec, int dir, int kind,
 /* acc_scan without any device allocation -- no counterpart in the reference,
  * which always allocates its temporaries (PTX/Execute.hs:453).  Same
  * arguments, results and errors as acc_scan, for callers that cannot let a
- * library call cudaMalloc: a host capturing the stream into a CUDA graph, an
- * integration with a fixed device-memory budget or its own pool allocator.
- * The look-back scratch lives in one file-scope device array of 2 MiB (plus
- * 256 bytes) that every GPU loading the library holds until the process
- * exits, so a row may have at most 2^28 elements; longer rows return
- * ACC_ERR_TOO_LARGE before anything is launched.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress): make that first
- * call before any stream capture.  Every call reuses the same array, so calls
+ * library call cudaMalloc: an integration that runs under a fixed
+ * device-memory budget, a plugin whose host process hands out all device
+ * memory from its own pool allocator, or a latency-bound loop that must not
+ * stall on cudaMalloc (which can synchronise the device).  The look-back
+ * scratch lives in one file-scope device array of 2 MiB (plus 256 bytes)
+ * that every GPU loading the library holds until the process exits, so a row
+ * may have at most 2^28 elements; longer rows return ACC_ERR_TOO_LARGE before
+ * anything is launched.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress): make that first call before any
+ * stream capture.  Each call clears the part of the array it uses, in stream
+ * order, before its kernel runs.  Every call reuses the same array, so calls
  * whose work overlaps on the GPU (other streams, other host threads) race and
  * must be serialised by the caller.  A look-back wait that runs out is not
  * reported by this entry point (acc_sync reports only acc_scan's workspaces);

@@ -59,6 +59,8 @@ def test_argument_validation_without_device(lib):
     one = ctypes.c_void_p(16)
     assert lib.acc_permute_clone(0, 0, one, N, one, one, 9, one, 4, 4, N) == 1  # rejected before the clone
     assert lib.acc_permute_clone(0, 0, one, N, N, one, 0, one, 4, 4, N) == 1   # no source, no constant
+    assert lib.acc_permute_clone(9, 0, one, N, one, one, 0, one, 4, 4, N) == 1   # no such primitive
+    assert lib.acc_permute_clone(4, 3, one, N, one, one, 0, one, 4, 4, N) == 2   # .&. on Float32
     assert lib.acc_stencil2d(3, 5, 1, N, 0, N, N, N, 4, 4, N) == 1         # radius > 4
     assert lib.acc_stencil2d(2, 1, 1, N, 0, N, N, N, 4, 4, N) == 2         # Word32 stencil unsupported
     assert lib.acc_fold_seg(0, 0, 0, N, N, 3, N, 1, 4, 2, N, N) == 1       # bad offset type

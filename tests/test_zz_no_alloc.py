@@ -1,12 +1,17 @@
 """acc_scan_noalloc: the scan entry point that performs no device allocation.
 
-It exists for hosts that cannot let the library call cudaMalloc (a stream under
-CUDA-graph capture, a fixed device-memory budget, an application-owned pool):
-its look-back scratch is a file-scope device array instead of a per-stream
-workspace.  These tests call it through the C ABI and compare it with acc_scan,
-two calls in a row (the array keeps the previous call's contents, so the
-second call checks that the per-call reset works).  Kept in a file that sorts
-last so that a failure here cannot hide the other tests.
+It exists for hosts that cannot let the library call cudaMalloc: an
+integration with a fixed device-memory budget, a host process that hands out
+all device memory from its own pool allocator, a loop that must not stall on
+cudaMalloc.  Its look-back scratch is a file-scope device array instead of a
+per-stream workspace.  These tests call it through the C ABI, two calls in a
+row (the array keeps the previous call's contents, so the second call checks
+that the per-call clearing works), and compare each result with the oracle
+and with acc_scan, within the tolerances of the scan tests: bit-exact for
+integers; Float32 (+) within 1e-6 |ref| + 1e-9 sum|x| of the FP64 oracle and
+Float64 (+) within 1e-12 sum|x| + 1e-15 |ref|.  One test checks that a call
+leaves the device's free memory unchanged.  Kept in a file that sorts last
+so that a failure here cannot hide the other tests.
 """
 import ctypes
 
@@ -16,32 +21,63 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-I32, I64, F32 = 0, 1, 3
+I32, I64, F32, F64 = 0, 1, 3, 4
+CT = {I32: ctypes.c_int32, I64: ctypes.c_int64, F32: ctypes.c_float, F64: ctypes.c_double}
 
 
-def _call(acc, fn, op, tcode, direction, kind, x, out, sums, outer, inner, seed):
+def _call(acc, fn, op, tcode, direction, kind, x, out, sums, outer, inner, seed, stream=None):
     sp = None
     keep = None
     if seed is not None:
-        keep = (ctypes.c_int64 if tcode == I64 else ctypes.c_float if tcode == F32 else ctypes.c_int32)(seed)
+        keep = CT[tcode](seed)
         sp = ctypes.cast(ctypes.pointer(keep), ctypes.c_void_p)
+    s = stream if stream is not None else torch.cuda.current_stream()
     st = fn(op, tcode, 0, direction, kind, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()),
             ctypes.c_void_p(sums.data_ptr()) if sums is not None else None, outer, inner, sp,
-            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+            ctypes.c_void_p(s.cuda_stream))
     return st
+
+
+def _oracle(orc, x, direction, kind, seed):
+    xs = x.cpu().numpy()
+    z = None if seed is None else xs.dtype.type(seed)
+    if xs.dtype.kind in "iu":
+        return orc.scan("+", z, xs, direction, kind), None
+    r64 = orc.scan_f64("+", None if seed is None else float(seed), xs, direction, kind)
+    a64 = orc.scan_f64("+", None if seed is None else abs(float(seed)), np.abs(xs), direction, kind)
+    return r64, a64
+
+
+def _check(got, got_sums, ref, ab, kind, dtype):
+    if ab is None:
+        if kind == 2:
+            assert np.array_equal(got, ref[0]) and np.array_equal(got_sums, ref[1])
+        else:
+            assert np.array_equal(got, ref)
+        return
+    pairs = [(got, ref[0], ab[0]), (got_sums, ref[1], ab[1])] if kind == 2 else [(got, ref, ab)]
+    for g, r, a in pairs:
+        err = np.abs(np.asarray(g, dtype=np.float64) - r)
+        if dtype == torch.float32:
+            tol = 1e-6 * np.abs(r) + 1e-9 * a
+        else:
+            tol = 1e-12 * a + 1e-15 * np.abs(r)
+        assert np.all(err <= tol + 1e-30), f"max excess {(err - tol).max()}"
 
 
 CASES = [
     # (dtype, type code, n, direction, kind, seed)
     (torch.int64, I64, (1 << 22) + 3, 0, 0, None),        # scanl1, many look-back tiles
+    (torch.int64, I64, (1 << 21) + 5, 1, 0, None),        # scanr1: the right-to-left look-back
     (torch.int32, I32, (1 << 21) + 17, 0, 1, 5),          # scanl z (n+1 outputs)
     (torch.int32, I32, 100_001, 1, 2, -3),                # scanr' z (+ totals)
     (torch.float32, F32, 1 << 21, 0, 0, None),            # compensated Float32 scanl1
+    (torch.float64, F64, (1 << 20) + 9, 1, 1, 0.25),      # Float64 scanr z
 ]
 
 
 @pytest.mark.parametrize("dtype,tcode,n,direction,kind,seed", CASES)
-def test_noalloc_matches_acc_scan_on_two_calls(acc, dev, dtype, tcode, n, direction, kind, seed):
+def test_noalloc_matches_oracle_and_acc_scan_on_two_calls(acc, orc, dev, dtype, tcode, n, direction, kind, seed):
     lib = acc.lib()
     g = torch.Generator(device=dev)
     g.manual_seed(n)
@@ -50,29 +86,47 @@ def test_noalloc_matches_acc_scan_on_two_calls(acc, dev, dtype, tcode, n, direct
     else:
         x = torch.randint(-1000, 1000, (n,), dtype=dtype, device=dev, generator=g)
     out_len = n + 1 if kind == 1 else n
-    ref = torch.empty(out_len, dtype=dtype, device=dev)
-    ref_sums = torch.empty(1, dtype=dtype, device=dev) if kind == 2 else None
-    assert _call(acc, lib.acc_scan, 0, tcode, direction, kind, x, ref, ref_sums, 1, n, seed) == 0
+    ref_gpu = torch.empty(out_len, dtype=dtype, device=dev)
+    ref_gpu_sums = torch.empty(1, dtype=dtype, device=dev) if kind == 2 else None
+    assert _call(acc, lib.acc_scan, 0, tcode, direction, kind, x, ref_gpu, ref_gpu_sums, 1, n, seed) == 0
     torch.cuda.synchronize()
+    ref, ab = _oracle(orc, x, direction, kind, seed)
     for _ in range(2):
         out = torch.full((out_len,), 7, dtype=dtype, device=dev)
         sums = torch.full((1,), 7, dtype=dtype, device=dev) if kind == 2 else None
         assert _call(acc, lib.acc_scan_noalloc, 0, tcode, direction, kind, x, out, sums, 1, n, seed) == 0
         torch.cuda.synchronize()
-        if dtype.is_floating_point:
-            # the tolerance of the Float32 (+) scan tests: 1e-6 |ref| + 1e-9 sum|x|
-            xs = x.double().cpu().numpy()
-            ab = np.cumsum(np.abs(xs))
-            r = ref.double().cpu().numpy()
-            err = np.abs(out.double().cpu().numpy() - r)
-            assert np.all(err <= 2 * (1e-6 * np.abs(r) + 1e-9 * ab) + 1e-30)
-        else:
-            assert torch.equal(out, ref)
-            if kind == 2:
-                assert torch.equal(sums, ref_sums)
+        got = out.cpu().numpy()
+        got_sums = sums.cpu().numpy() if sums is not None else None
+        _check(got, got_sums, ref, ab, kind, dtype)
+        # the entry point it stands in for: the same kernels, so the same bits
+        assert torch.equal(out, ref_gpu)
+        if kind == 2:
+            assert torch.equal(sums, ref_gpu_sums)
 
 
-def test_noalloc_rows_and_empty(acc, dev):
+def test_noalloc_leaves_free_device_memory_unchanged(acc, orc, dev):
+    lib = acc.lib()
+    n_small, n_big = 1 << 16, (1 << 24) + 7
+    x = torch.randint(-9, 9, (n_big,), dtype=torch.int64, device=dev)
+    out = torch.empty(n_big, dtype=torch.int64, device=dev)
+    # A first call on this device (looks up the array's address and loads the
+    # kernel) on a small input ...
+    assert _call(acc, lib.acc_scan_noalloc, 0, I64, 0, 0, x, out, None, 1, n_small, None) == 0
+    torch.cuda.synchronize()
+    # ... then a call on a stream no library call has used before, with more
+    # look-back tiles than any earlier call: acc_scan would create and grow a
+    # workspace for it here.
+    s = torch.cuda.Stream()
+    free0, _ = torch.cuda.mem_get_info()
+    assert _call(acc, lib.acc_scan_noalloc, 0, I64, 0, 0, x, out, None, 1, n_big, None, stream=s) == 0
+    s.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert np.array_equal(out.cpu().numpy(), orc.scan("+", None, x.cpu().numpy(), 0, 0))
+
+
+def test_noalloc_rows_and_empty(acc, orc, dev):
     lib = acc.lib()
     x = torch.randint(-50, 50, (3, 1000), dtype=torch.int32, device=dev)
     ref = torch.empty((3, 1001), dtype=torch.int32, device=dev)
@@ -81,6 +135,7 @@ def test_noalloc_rows_and_empty(acc, dev):
     assert _call(acc, lib.acc_scan_noalloc, 0, I32, 0, 1, x, out, None, 3, 1000, 4) == 0
     torch.cuda.synchronize()
     assert torch.equal(out, ref)
+    assert np.array_equal(out.cpu().numpy(), orc.scan("+", np.int32(4), x.cpu().numpy(), 0, 1))
     e = torch.empty(0, dtype=torch.int32, device=dev)
     o = torch.empty(1, dtype=torch.int32, device=dev)
     assert _call(acc, lib.acc_scan_noalloc, 0, I32, 0, 1, e, o, None, 1, 0, 9) == 0

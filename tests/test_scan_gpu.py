@@ -82,6 +82,15 @@ def test_scan_sizes(acc, orc, dev, t, op, n):
         run_scan(acc, orc, dev, t, op, (n,), d, k)
 
 
+# Arrays of hundreds of tiles: look-backs that span several windows, a
+# partial last tile, and a tile count that is a multiple of the SM count.
+@pytest.mark.parametrize("t,op,n", [("i32", "+", (1 << 23) + 3), ("i32", "+", 608 * 8192), ("u32", "xor", 1 << 23),
+                                    ("i64", "+", (1 << 22) + 5), ("f32", "+", (1 << 23) + 1), ("f64", "max", 3 << 20)])
+def test_scan_large_sizes(acc, orc, dev, t, op, n):
+    for d, k in FLAVOURS:
+        run_scan(acc, orc, dev, t, op, (n,), d, k)
+
+
 @pytest.mark.parametrize("t,op", [("i32", "+"), ("f32", "+"), ("i64", "max"), ("f64", "+")])
 @pytest.mark.parametrize("shape", [(3, 1000), (1000, 3), (2, 9000), (64, 1), (5, 4096)])
 def test_scan_rows(acc, orc, dev, t, op, shape):
@@ -126,9 +135,10 @@ def test_scan_empty(acc, dev):
     assert acc.scanl("+", 9, e2).cpu().tolist() == [[9], [9], [9]]
 
 
-def test_scan_in_place(acc, orc, dev):
+@pytest.mark.parametrize("n", [300_001, (1 << 22) + 1])
+def test_scan_in_place(acc, orc, dev, n):
     rng = np.random.default_rng(5)
-    x = rng.integers(-100, 100, size=300_001).astype(np.int64)
+    x = rng.integers(-100, 100, size=n).astype(np.int64)
     td = torch.from_numpy(x).to(dev)
     st = acc.lib().acc_scan(0, 1, 0, 0, 0, acc._ptr(td), acc._ptr(td), None, 1, td.numel(), None, acc._stream())
     assert st == 0

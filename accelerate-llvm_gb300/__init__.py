@@ -7,7 +7,11 @@ PTX/Execute.hs:83-109) with the Accelerate names and argument meaning:
 
     fold f z xs, fold1 f xs, fold_seg f z xs seg, fold1_seg f xs seg,
     scanl/scanl1/scanr/scanr1, scanl_ (scanl'), scanr_ (scanr'),
-    permute f defaults idx xs, stencil (weighted sum) and stencil2.
+    permute f defaults idx xs, stencil (weighted sum) and stencil2,
+
+plus the host <-> device transfers (``upload`` / ``download``, pokeArrayAsync /
+peekArrayAsync) and the memory table (``Table``: useArrayAsync, mallocArray,
+pokeArrayAsync, peekArrayAsync, withRemote, freeRemote).
 
 Arrays are CUDA tensors (torch is the device allocator and stream provider
 only); results are allocated here, as the reference allocates them with
@@ -75,6 +79,7 @@ SIGNATURES = {
     "acc_strerror": ([_I], ctypes.c_char_p),
     "acc_sync": ([_P], _I),
     "acc_release_workspaces": ([], _I),
+    "acc_selftest_timeout": ([_I, _P], _I),
     "acc_fold": ([_I, _I, _I, _P, _P, _L, _L, _P, _P], _I),
     "acc_fold_zipwith": ([_I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_fold_seg": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
@@ -82,7 +87,10 @@ SIGNATURES = {
     "acc_fold_seg_lengths": ([_I, _I, _I, _P, _P, _I, _P, _L, _L, _L, _P, _P], _I),
     "acc_scan": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_scan_noalloc": ([_I, _I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
+    "acc_scan_noalloc_status": ([_P], _I),
     "acc_scan_zipwith": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _L, _L, _P, _P], _I),
+    "acc_scan_map": ([_I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _L, _L, _P, _P], _I),
+    "acc_fold_map": ([_I, _I, _I, _I, _P, _P, _P, _L, _L, _P, _P], _I),
     "acc_permute": ([_I, _I, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_permute_clone": ([_I, _I, _P, _P, _P, _P, _I, _P, _L, _L, _P], _I),
     "acc_stencil2d": ([_I, _I, _I, _P, _I, _P, _P, _P, _L, _L, _P], _I),
@@ -96,6 +104,21 @@ SIGNATURES = {
     "acc_batch_autotune": ([ctypes.c_char_p, _P], _I),
     "acc_batch_load_tuning": ([ctypes.c_char_p], _I),
     "acc_serve_run": ([_P, _L, _L, _I, _I, _P, _P], _I),
+    "acc_upload": ([_P, _P, _L, _P], _I),
+    "acc_download": ([_P, _P, _L, _P], _I),
+    "acc_table_create": ([_L, _P], _I),
+    "acc_table_destroy": ([_P], _I),
+    "acc_table_use": ([_P, _P, _L, _P, _P], _I),
+    "acc_table_malloc": ([_P, _P, _L, _P, _P], _I),
+    "acc_table_poke": ([_P, _P, _P], _I),
+    "acc_table_peek": ([_P, _P, _P], _I),
+    "acc_table_release": ([_P, _P, _P], _I),
+    "acc_table_wait": ([_P, _P], _I),
+    "acc_table_join": ([_P, _P], _I),
+    "acc_table_free": ([_P, _P], _I),
+    "acc_table_get_stats": ([_P, _P], _I),
+    "acc_table_trace": ([_P, _I], _I),
+    "acc_table_trace_get": ([_P, _P, _P, _L, _P], _I),
 }
 
 
@@ -236,6 +259,28 @@ def fold_zipwith(f, g, z, xs: torch.Tensor, ys: torch.Tensor, prec=None, stream=
     return out
 
 
+def fold_map(f, g, c, z, xs: torch.Tensor, prec=None, stream=None) -> torch.Tensor:
+    """fold f z (map (\\x -> g x c) xs) with the map fused into the fold (the
+    reference's delayed fold input, PTX/CodeGen/Fold.hs:80-97); z = None gives
+    fold1.  The reference's known answer sum (map (+1) xs) is
+    fold_map("+", "+", 1, 0, xs)."""
+    xs = _dev(xs)
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1] if shape else 1
+    outer_shape = shape[:-1]
+    outer = 1
+    for d in outer_shape:
+        outer *= d
+    out = torch.empty(outer_shape, dtype=xs.dtype, device=xs.device)
+    sp, _keep = _seed_ptr(tc, z)
+    cp, _keep_c = _seed_ptr(tc, c)
+    st = lib().acc_fold_map(op_of(f), op_of(g), tc, PRECS[prec], _ptr(xs), cp, _ptr(out), outer, inner, sp,
+                            _stream(stream))
+    _check(st, "fold_map")
+    return out
+
+
 def dotp(xs: torch.Tensor, ys: torch.Tensor, prec=None, stream=None) -> torch.Tensor:
     """dotp xs ys = fold (+) 0 (zipWith (*) xs ys)."""
     return fold_zipwith("+", "*", 0, xs, ys, prec=prec, stream=stream)
@@ -365,6 +410,29 @@ def scan_zipwith(flavour, f, g, z, xs: torch.Tensor, ys: torch.Tensor, prec=None
     st = lib().acc_scan_zipwith(op_of(f), op_of(g), tc, PRECS[prec], direction, kind, _ptr(xs), _ptr(ys), _ptr(out),
                                 _ptr(sums) if sums is not None else None, outer, inner, sp, _stream(stream))
     _check(st, "scan_zipwith")
+    return (out, sums) if kind == SCAN_PRIME else out
+
+
+def scan_map(flavour, f, g, c, z, xs: torch.Tensor, prec=None, stream=None):
+    """A scan of the fused producer map (\\x -> g x c) xs, e.g.
+    scan_map("scanl1", "+", "+", 1, None, xs) = scanl1 (+) (map (+1) xs).  The
+    mapped array is never written (acc_scan_map)."""
+    direction, kind = _SCAN_FLAVOURS[flavour]
+    xs = _dev(xs)
+    tc = type_of(xs)
+    shape = tuple(xs.shape)
+    inner = shape[-1]
+    outer = 1
+    for d in shape[:-1]:
+        outer *= d
+    out_inner = inner + 1 if kind == SCAN_SEEDED else inner
+    out = torch.empty(shape[:-1] + (out_inner,), dtype=xs.dtype, device=xs.device)
+    sums = torch.empty(shape[:-1], dtype=xs.dtype, device=xs.device) if kind == SCAN_PRIME else None
+    sp, _keep = _seed_ptr(tc, None if kind == SCAN_INCLUSIVE else z)
+    cp, _keep_c = _seed_ptr(tc, c)
+    st = lib().acc_scan_map(op_of(f), op_of(g), tc, PRECS[prec], direction, kind, _ptr(xs), cp, _ptr(out),
+                            _ptr(sums) if sums is not None else None, outer, inner, sp, _stream(stream))
+    _check(st, "scan_map")
     return (out, sums) if kind == SCAN_PRIME else out
 
 
@@ -506,7 +574,7 @@ class Batch:
             arr[i].kind = REQ_FOLD if kind == "fold" else REQ_SCAN
             arr[i].type = tc
             arr[i].inp = xs.data_ptr()
-            arr[i].out = out.data_ptr()
+            arr[i].out = out.data_ptr() if out is not None else 0
             arr[i].n = xs.numel()
             arr[i].has_seed = 0 if seed is None else 1
             arr[i].seed = 0 if seed is None else _seed_bits(tc, seed)
@@ -554,7 +622,7 @@ class ServeReq(ctypes.Structure):
     """struct acc_serve_req of acc_gb300.h."""
     _fields_ = [("skeleton", ctypes.c_int), ("type", ctypes.c_int), ("inp", ctypes.c_void_p),
                 ("aux", ctypes.c_void_p), ("out", ctypes.c_void_p), ("n", ctypes.c_int64), ("m", ctypes.c_int64),
-                ("arrival", ctypes.c_double)]
+                ("arrival", ctypes.c_double), ("host_out", ctypes.c_void_p)]
 
 
 class ServeStats(ctypes.Structure):
@@ -564,12 +632,17 @@ class ServeStats(ctypes.Structure):
 
 def serve(requests, budget_bytes: int, slots: int = 8, mode: str = "batching"):
     """Serve a request stream (acc_serve_run).  `requests`: list of
-    (skeleton name, input tensor, aux tensor or None, output tensor, n, m,
-    arrival seconds), sorted by arrival.  Returns (latencies in seconds as a
-    list, stats dict)."""
+    (skeleton name, input tensor, aux tensor or None, output tensor or None,
+    n, m, arrival seconds[, host array or None]), sorted by arrival.  A None
+    output places the result in the loop's device arena of `budget_bytes`
+    (admission waits until it fits); a host array (numpy or CPU tensor)
+    receives a copy of the result.  Returns (latencies in seconds as a list,
+    stats dict)."""
     arr = (ServeReq * max(1, len(requests)))()
     keep = []
-    for i, (sk, xs, aux, out, n, m, t) in enumerate(requests):
+    for i, req in enumerate(requests):
+        sk, xs, aux, out, n, m, t = req[:7]
+        host_out = req[7] if len(req) > 7 else None
         if sk not in SKELETONS:
             raise ValueError(f"request {i}: skeleton {sk!r}, expected one of {sorted(SKELETONS)}")
         if n < 0 or m < 0:
@@ -577,20 +650,29 @@ def serve(requests, budget_bytes: int, slots: int = 8, mode: str = "batching"):
         what = f"request {i} ({sk})"
         if sk == "permute":
             _given(xs, n, what + " indices", torch.int32)
-            _given(out, m, what + " bins", torch.int32)
+            if out is not None:
+                _given(out, m, what + " bins", torch.int32)
         else:
             _given(xs, n * m if sk == "stencil" else n, what + " input")
             if sk == "stencil" and xs.dtype not in (torch.float32, torch.float64):
                 raise TypeError(f"{what}: the 5-point stencil takes Float32 / Float64 grids")
-            _given(out, {"fold": 1, "scan": n, "foldseg": m, "stencil": n * m}[sk], what + " output", xs.dtype)
+            if out is not None:
+                _given(out, {"fold": 1, "scan": n, "foldseg": m, "stencil": n * m}[sk], what + " output", xs.dtype)
         if sk == "foldseg":
             _given(aux, m + 1, what + " offsets", torch.int32)
-        keep += [xs, aux, out]
+        esz = 4 if sk == "permute" else xs.element_size()
+        nres = {"fold": 1, "scan": n, "foldseg": m, "permute": m, "stencil": n * m}[sk]
+        if host_out is not None:
+            haddr, hbytes = _host_buf(host_out)
+            if hbytes < nres * esz:
+                raise ValueError(f"{what}: host_out holds {hbytes} bytes, {nres * esz} needed")
+            arr[i].host_out = haddr
+        keep += [xs, aux, out, host_out]
         arr[i].skeleton = SKELETONS[sk]
         arr[i].type = type_of(xs) if sk != "permute" else I32
         arr[i].inp = xs.data_ptr()
         arr[i].aux = aux.data_ptr() if aux is not None else 0
-        arr[i].out = out.data_ptr()
+        arr[i].out = out.data_ptr() if out is not None else 0
         arr[i].n = n
         arr[i].m = m
         arr[i].arrival = t
@@ -601,3 +683,159 @@ def serve(requests, budget_bytes: int, slots: int = 8, mode: str = "batching"):
                              ctypes.cast(ctypes.pointer(stats), ctypes.c_void_p))
     _check(st, "acc_serve_run")
     return list(lat)[:len(requests)], {k: getattr(stats, k) for k, _ in ServeStats._fields_}
+
+
+# ----------------------------------------------------------------- transfers and the memory table
+def _host_buf(h):
+    """(address, bytes) of a contiguous host array: a numpy array or a CPU
+    tensor, pinned or pageable."""
+    if isinstance(h, torch.Tensor):
+        if h.is_cuda:
+            raise ValueError("host arrays must be in host memory")
+        if not h.is_contiguous():
+            raise ValueError("host arrays must be contiguous")
+        return h.data_ptr(), h.numel() * h.element_size()
+    import numpy as np
+    if not isinstance(h, np.ndarray):
+        raise TypeError(f"unsupported host array {type(h).__name__}")
+    if not h.flags["C_CONTIGUOUS"]:
+        raise ValueError("host arrays must be contiguous")
+    return h.ctypes.data, h.nbytes
+
+
+def upload(dev: torch.Tensor, host, stream=None) -> None:
+    """pokeArrayAsync on caller-owned device memory (acc_upload): enqueue the
+    copy of the host array into `dev` on the stream."""
+    addr, nbytes = _host_buf(host)
+    if dev.numel() * dev.element_size() < nbytes or not dev.is_cuda or not dev.is_contiguous():
+        raise ValueError("upload: the device array must be contiguous and hold the host array")
+    _check(lib().acc_upload(_ptr(dev), ctypes.c_void_p(addr), nbytes, _stream(stream)), "acc_upload")
+
+
+def download(host, dev: torch.Tensor, stream=None) -> None:
+    """peekArrayAsync on caller-owned device memory (acc_download): enqueue the
+    copy of `dev` into the host array on the stream (acc_sync before reading)."""
+    addr, nbytes = _host_buf(host)
+    if dev.numel() * dev.element_size() < nbytes or not dev.is_cuda or not dev.is_contiguous():
+        raise ValueError("download: the device array must be contiguous and hold the host array")
+    _check(lib().acc_download(ctypes.c_void_p(addr), _ptr(dev), nbytes, _stream(stream)), "acc_download")
+
+
+class XferRecord(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("bytes", ctypes.c_int64), ("start_ms", ctypes.c_double),
+                ("end_ms", ctypes.c_double)]
+
+
+class TableStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("budget", "resident_bytes", "arrays", "uploads", "upload_bytes",
+                                              "downloads", "download_bytes", "hits", "evictions", "writebacks")]
+
+
+class _DeviceView:
+    """A device range of the table's arena, exposed to torch without a copy."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+_TYPESTR = {torch.int32: "<i4", torch.int64: "<i8", torch.float32: "<f4", torch.float64: "<f8"}
+
+
+def _typestr(h):
+    """(typestr, shape) of the device view of a host array: its own element
+    type and shape, or raw bytes for an element type outside the skeletons'."""
+    if isinstance(h, torch.Tensor):
+        if h.dtype in _TYPESTR:
+            return _TYPESTR[h.dtype], tuple(h.shape)
+        return "|u1", (h.numel() * h.element_size(),)
+    return h.dtype.str, tuple(h.shape)
+
+
+class Table:
+    """The memory table (acc_table_*): device copies of host arrays in one
+    device arena of `budget_bytes`, least recently used first out.
+
+    Mirrors the reference's memory table and transfers
+    (PTX/Array/Table.hs:35-49, PTX/Array/Remote.hs:60-133,
+    PTX/Array/Prim.hs:72-195): ``use`` (useArrayAsync: upload unless
+    resident), ``malloc`` (mallocArray: space for an output), ``poke`` /
+    ``peek`` (pokeArrayAsync / peekArrayAsync), ``release`` (the end of a
+    withRemote), ``wait`` and ``free`` (freeRemote).  ``use`` and ``malloc``
+    return a CUDA tensor that views the device copy (no allocation, no copy);
+    it is valid until the array is evicted, i.e. while held."""
+
+    def __init__(self, budget_bytes: int):
+        h = ctypes.c_void_p()
+        _check(lib().acc_table_create(int(budget_bytes), ctypes.byref(h)), "acc_table_create")
+        self._h = h
+
+    def _view(self, ptr, host):
+        typestr, shape = _typestr(host)
+        return torch.as_tensor(_DeviceView(ptr.value or 0, shape, typestr), device=torch.device("cuda", torch.cuda.current_device()))
+
+    def use(self, host, stream=None) -> torch.Tensor:
+        addr, nbytes = _host_buf(host)
+        p = ctypes.c_void_p()
+        _check(lib().acc_table_use(self._h, ctypes.c_void_p(addr), nbytes, _stream(stream), ctypes.byref(p)),
+               "acc_table_use")
+        return self._view(p, host)
+
+    def malloc(self, host, stream=None) -> torch.Tensor:
+        addr, nbytes = _host_buf(host)
+        p = ctypes.c_void_p()
+        _check(lib().acc_table_malloc(self._h, ctypes.c_void_p(addr), nbytes, _stream(stream), ctypes.byref(p)),
+               "acc_table_malloc")
+        return self._view(p, host)
+
+    def poke(self, host, stream=None) -> None:
+        _check(lib().acc_table_poke(self._h, ctypes.c_void_p(_host_buf(host)[0]), _stream(stream)), "acc_table_poke")
+
+    def peek(self, host, stream=None) -> None:
+        _check(lib().acc_table_peek(self._h, ctypes.c_void_p(_host_buf(host)[0]), _stream(stream)), "acc_table_peek")
+
+    def release(self, host, stream=None) -> None:
+        _check(lib().acc_table_release(self._h, ctypes.c_void_p(_host_buf(host)[0]), _stream(stream)),
+               "acc_table_release")
+
+    def wait(self, host) -> None:
+        _check(lib().acc_table_wait(self._h, ctypes.c_void_p(_host_buf(host)[0])), "acc_table_wait")
+
+    def join(self, stream=None) -> None:
+        """Make the stream wait for every transfer enqueued on the table so far."""
+        _check(lib().acc_table_join(self._h, _stream(stream)), "acc_table_join")
+
+    def free(self, host) -> None:
+        _check(lib().acc_table_free(self._h, ctypes.c_void_p(_host_buf(host)[0])), "acc_table_free")
+
+    def stats(self) -> dict:
+        st = TableStats()
+        _check(lib().acc_table_get_stats(self._h, ctypes.byref(st)), "acc_table_get_stats")
+        return {n: getattr(st, n) for n, _ in TableStats._fields_}
+
+    def trace(self, enable: bool = True) -> None:
+        """Start (or stop) timing every transfer of the table; clears the trace."""
+        _check(lib().acc_table_trace(self._h, 1 if enable else 0), "acc_table_trace")
+
+    def trace_records(self, origin) -> list:
+        """The traced transfers as (kind, bytes, start ms, end ms) after the
+        `origin` event (a torch.cuda.Event with timing, recorded before them)."""
+        cnt = ctypes.c_int64()
+        _check(lib().acc_table_trace_get(self._h, ctypes.c_void_p(origin.cuda_event), None, 0, ctypes.byref(cnt)),
+               "acc_table_trace_get")
+        recs = (XferRecord * max(1, cnt.value))()
+        _check(lib().acc_table_trace_get(self._h, ctypes.c_void_p(origin.cuda_event), recs, cnt.value,
+                                         ctypes.byref(cnt)), "acc_table_trace_get")
+        kinds = {0: "upload", 1: "download", 2: "copy back"}
+        return [(kinds.get(r.kind, r.kind), r.bytes, r.start_ms, r.end_ms) for r in recs[:cnt.value]]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            h, self._h = self._h, None
+            _check(lib().acc_table_destroy(h), "acc_table_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -197,12 +197,15 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
         uint32_t flag = exists ? 0u : 2u;
         S v = A::id();
         uint32_t it = 0;
+        uint64_t t_wait = 0;
         while (true) {
           if (exists && flag == 0) flag = b_peek<S>(a.status, pt, epoch, v);
           if (__all_sync(0xffffffffu, flag != 0)) break;
           ++it;
+          if (it == 1) t_wait = global_ns();
           const bool stop = gave_up || it > SPIN_LIMIT ||
-                            ((it & 63u) == 0 && (ld_relaxed_u32(a.words) & DEV_ERR_TIMEOUT) != 0u);
+                            ((it & 63u) == 0 && ((ld_relaxed_u32(a.words) & DEV_ERR_TIMEOUT) != 0u ||
+                                                 global_ns() - t_wait > WAIT_LIMIT_NS));
           if (__any_sync(0xffffffffu, stop)) {
             gave_up = true;
             if (lane == 0) raise_error(a.words, DEV_ERR_TIMEOUT);

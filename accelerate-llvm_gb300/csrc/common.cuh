@@ -18,9 +18,18 @@
 namespace accgb {
 
 // ----------------------------------------------------------------- errors
-// Upper bound on the spin iterations of any wait on another CTA
-// (each iteration sleeps up to 256 ns: the bound is a few seconds at most).
+// Every wait on another CTA or on a copy is bounded: it gives up after
+// WAIT_LIMIT_NS of wall-clock time (%globaltimer), or after SPIN_LIMIT polls,
+// whichever comes first.  The poll count alone is no time bound: a poll may
+// suspend for microseconds (mbarrier.try_wait) or sleep longer than asked.
 constexpr uint32_t SPIN_LIMIT = 1u << 24;
+constexpr uint64_t WAIT_LIMIT_NS = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // ----------------------------------------------------------------- ops
 template <int OP, class T> struct Prim;
@@ -381,6 +390,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
 // Bounded wait on an mbarrier phase.  Returns false if the wait gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
   uint32_t addr = smem_addr(bar);
+  uint64_t t0 = 0;
   for (uint32_t it = 0; it < SPIN_LIMIT; ++it) {
     uint32_t done;
     asm volatile(
@@ -389,17 +399,32 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done) : "r"(addr), "r"(phase) : "memory");
     if (done) return true;
-    if (it > 64) __nanosleep(64);
+    if (it == 0) t0 = global_ns();
+    if (it > 64) {
+      if ((it & 15u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) return false;
+      __nanosleep(64);
+    }
   }
   return false;
+}
+// Bounded wait for a TMA load's mbarrier phase.  A wait that runs out raises
+// DEV_ERR_TIMEOUT and waits once more (again bounded), so that a copy still
+// in flight has twice the limit to land.  Returns whether the phase
+// completed.  The caller makes the outcome CTA-uniform (__syncthreads_or)
+// and, when the load did not land, returns without reading the buffer, without
+// storing from it and without issuing another copy into it.
+__device__ __forceinline__ bool mbar_wait_flagged(uint64_t *bar, uint32_t phase, uint32_t *err) {
+  if (mbar_wait(bar, phase)) return true;
+  raise_error(err, DEV_ERR_TIMEOUT);
+  return mbar_wait(bar, phase);
 }
 // Bounded wait on an mbarrier phase that suspends the waiting threads (each
 // try may sleep up to 2 us until the phase completes) instead of polling, so
 // that waiting warps leave the issue slots to the CTAs that have work.  Gives
-// up after 2^20 tries (tens of milliseconds at the least, about two seconds
-// at most).  Returns false if it gave up.
+// up after WAIT_LIMIT_NS or 2^20 tries.  Returns false if it gave up.
 __device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t phase) {
   uint32_t addr = smem_addr(bar);
+  uint64_t t0 = 0;
   for (uint32_t it = 0; it < (1u << 20); ++it) {
     uint32_t done;
     asm volatile(
@@ -408,6 +433,8 @@ __device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t phase) {
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done) : "r"(addr), "r"(phase), "r"(2000u) : "memory");
     if (done) return true;
+    if (it == 0) t0 = global_ns();
+    if ((it & 15u) == 15u && global_ns() - t0 > WAIT_LIMIT_NS) return false;
     if (it > 8) __nanosleep(128);  // in case a try returns early
   }
   return false;
@@ -426,6 +453,28 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, int x, int 
 __device__ __forceinline__ void tma_store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void tma_store_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void tma_store_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// Plain arrival on an mbarrier (no transaction bytes).
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(bar)) : "memory");
+}
+// Barrier among the first THREADS threads of the CTA only (named barrier ID,
+// 1..15; 0 is __syncthreads), so that warps with other roles take no part.
+template <int ID, int THREADS>
+__device__ __forceinline__ void named_bar_sync() {
+  asm volatile("bar.sync %0, %1;" :: "n"(ID), "n"(THREADS) : "memory");
+}
+// The same barrier, returning whether v holds in any of those threads.
+template <int ID, int THREADS>
+__device__ __forceinline__ bool named_bar_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r) : "r"((uint32_t)v), "n"(ID), "n"(THREADS) : "memory");
+  return r != 0u;
+}
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" :: "l"(map) : "memory");
 }

@@ -1,20 +1,5 @@
-// fold.cu -- fold f z / fold1 f along the innermost dimension.
-//
-// The reference reduces a vector with a host-driven chain of launches
-// (foldAllM1, then foldAllM2 re-launched until one element is left:
-// accelerate-llvm-ptx/src/Data/Array/Accelerate/LLVM/PTX/Execute.hs:267-318,
-// PTX/CodeGen/Fold.hs:175-285) and a rank >= 2 array with one CTA per row
-// (Fold.hs:296-405).  Here every shape is one launch:
-//   * fold_rows_thread  -- inner <= 16: one thread per row;
-//   * fold_rows_warp    -- short rows, many of them: one warp per row;
-//   * fold_split        -- long rows: a row is cut over G CTAs, each thread
-//                          streams 16-byte vectors (4 in flight), the CTA
-//                          partial goes to scratch, and the last CTA of the
-//                          row (atomic ticket) folds the G partials in order
-//                          and applies the seed.
-// The seed combines on the left, z `f` (x0 `f` ...), as reduceFromTo does
-// (accelerate-llvm-native/.../Native/CodeGen/Fold.hs:248-260).  Float32 (+)
-// accumulates with a compensated two-sum by default.
+// fold.cu -- the C ABI of fold f z / fold1 f along the innermost dimension;
+// the kernels and their design are in fold_impl.cuh.
 #include "fold_impl.cuh"
 
 

@@ -1,5 +1,5 @@
 // fold_impl.cuh -- the fold kernels, shared by acc_fold (fold.cu) and the
-// fused-producer fold acc_fold_zipwith (fold_zip.cu).
+// fused-producer folds acc_fold_zipwith and acc_fold_map (fold_zip.cu).
 //
 // The reference reduces a vector with a host-driven chain of launches
 // (foldAllM1, then foldAllM2 re-launched until one element is left:
@@ -22,14 +22,20 @@
 namespace accgb {
 
 
-// The folded input: one array (ZOP = NO_ZIP), or the fused producer
-// `zipWith zop p q` of two arrays of the same shape, for a primitive zop.
+// The folded input: one array (ZOP = NO_ZIP), the fused producer
+// `zipWith zop p q` of two arrays of the same shape for a primitive zop
+// (ZOP < MAP_BASE), or the fused producer `map (\x -> g x c) p` for a
+// primitive g = ZOP - MAP_BASE and a constant c (ZOP >= MAP_BASE).
 constexpr int NO_ZIP = -1;
+constexpr int MAP_BASE = 16;
+template <int ZOP> constexpr bool zips() { return ZOP != NO_ZIP && ZOP < MAP_BASE; }
+template <int ZOP> constexpr bool maps() { return ZOP >= MAP_BASE; }
 
 template <int ZOP, class T>
-__device__ __forceinline__ T zip_at(const T *p, const T *q, int64_t i) {
-  if constexpr (ZOP == NO_ZIP) { (void)q; return ld_stream(p + i); }
-  else return Prim<ZOP, T>::ap(ld_stream(p + i), ld_stream(q + i));
+__device__ __forceinline__ T zip_at(const T *p, const T *q, int64_t i, T c) {
+  if constexpr (ZOP == NO_ZIP) { (void)q; (void)c; return ld_stream(p + i); }
+  else if constexpr (maps<ZOP>()) { (void)q; return Prim<ZOP - MAP_BASE, T>::ap(ld_stream(p + i), c); }
+  else { (void)c; return Prim<ZOP, T>::ap(ld_stream(p + i), ld_stream(q + i)); }
 }
 
 // Fold the span [0, len) of the input as participant t of nt (16-byte vector
@@ -38,31 +44,35 @@ __device__ __forceinline__ T zip_at(const T *p, const T *q, int64_t i) {
 // alignment phase, and a scalar stride otherwise.
 template <class A, class T, int ZOP = NO_ZIP>
 __device__ __forceinline__ typename A::S reduce_span(const T *p, int64_t len, int64_t t, int64_t nt,
-                                                     const T *q = nullptr) {
+                                                     const T *q = nullptr, T c = T{}) {
   using S = typename A::S;
   constexpr int VEC = 16 / sizeof(T);
   S acc = A::id();
   const uintptr_t addr = reinterpret_cast<uintptr_t>(p);
-  if constexpr (ZOP != NO_ZIP) {
+  if constexpr (zips<ZOP>()) {
     if (((addr ^ reinterpret_cast<uintptr_t>(q)) & 15u) != 0u) {
-      for (int64_t i = t; i < len; i += nt) acc = A::push(acc, zip_at<ZOP, T>(p, q, i));
+      for (int64_t i = t; i < len; i += nt) acc = A::push(acc, zip_at<ZOP, T>(p, q, i, c));
       return acc;
     }
   }
   int64_t head = (int64_t)(((16u - (addr & 15u)) & 15u) / sizeof(T));
   if (head > len) head = len;
-  if (t < head) acc = A::push(acc, zip_at<ZOP, T>(p, q, t));
+  if (t < head) acc = A::push(acc, zip_at<ZOP, T>(p, q, t, c));
   const int64_t nvec = (len - head) / VEC;
   const uint4 *pv = reinterpret_cast<const uint4 *>(p + head);
   const uint4 *qv = reinterpret_cast<const uint4 *>(q + head);
   auto push_vec = [&](const uint4 &v, const uint4 &w) {
     T e[VEC];
     memcpy(e, &v, 16);
-    if constexpr (ZOP != NO_ZIP) {
+    if constexpr (zips<ZOP>()) {
       T f[VEC];
       memcpy(f, &w, 16);
 #pragma unroll
       for (int k = 0; k < VEC; ++k) e[k] = Prim<ZOP, T>::ap(e[k], f[k]);
+    } else if constexpr (maps<ZOP>()) {
+      (void)w;
+#pragma unroll
+      for (int k = 0; k < VEC; ++k) e[k] = Prim<ZOP - MAP_BASE, T>::ap(e[k], c);
     } else {
       (void)w;
     }
@@ -75,7 +85,7 @@ __device__ __forceinline__ typename A::S reduce_span(const T *p, int64_t len, in
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       v[u] = ld_stream16(pv + i + u * nt);
-      if constexpr (ZOP != NO_ZIP) w[u] = ld_stream16(qv + i + u * nt);
+      if constexpr (zips<ZOP>()) w[u] = ld_stream16(qv + i + u * nt);
       else w[u] = v[u];
     }
 #pragma unroll
@@ -84,11 +94,11 @@ __device__ __forceinline__ typename A::S reduce_span(const T *p, int64_t len, in
   for (; i < nvec; i += nt) {
     const uint4 v = ld_stream16(pv + i);
     uint4 w = v;
-    if constexpr (ZOP != NO_ZIP) w = ld_stream16(qv + i);
+    if constexpr (zips<ZOP>()) w = ld_stream16(qv + i);
     push_vec(v, w);
   }
   const int64_t tail0 = head + nvec * VEC;
-  if (tail0 + t < len) acc = A::push(acc, zip_at<ZOP, T>(p, q, tail0 + t));
+  if (tail0 + t < len) acc = A::push(acc, zip_at<ZOP, T>(p, q, tail0 + t, c));
   return acc;
 }
 
@@ -117,6 +127,7 @@ struct FoldArgs {
   int64_t outer, inner;
   uint64_t seed;
   int has_seed;
+  uint64_t mapc;    // the constant of a fused map (bits of one element)
 };
 
 template <int OP, class T, int PREC, int ZOP = NO_ZIP>
@@ -127,9 +138,10 @@ __global__ void __launch_bounds__(256) fold_rows_thread(FoldArgs a) {
   T *out = static_cast<T *>(a.out);
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.outer; r += (int64_t)gridDim.x * blockDim.x) {
     const T *p = in + r * a.inner;
-    const T *q = ZOP == NO_ZIP ? nullptr : in2 + r * a.inner;
-    typename A::S acc = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::lift(zip_at<ZOP, T>(p, q, 0));
-    for (int64_t i = a.has_seed ? 0 : 1; i < a.inner; ++i) acc = A::push(acc, zip_at<ZOP, T>(p, q, i));
+    const T *q = zips<ZOP>() ? in2 + r * a.inner : nullptr;
+    const T c = from_bits<T>(a.mapc);
+    typename A::S acc = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::lift(zip_at<ZOP, T>(p, q, 0, c));
+    for (int64_t i = a.has_seed ? 0 : 1; i < a.inner; ++i) acc = A::push(acc, zip_at<ZOP, T>(p, q, i, c));
     out[r] = A::lower(acc);
   }
 }
@@ -145,7 +157,7 @@ __global__ void __launch_bounds__(256) fold_rows_warp(FoldArgs a) {
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t r = gw; r < a.outer; r += nw) {
     typename A::S acc = reduce_span<A, T, ZOP>(in + r * a.inner, a.inner, lane, 32,
-                                               ZOP == NO_ZIP ? nullptr : in2 + r * a.inner);
+                                               zips<ZOP>() ? in2 + r * a.inner : nullptr, from_bits<T>(a.mapc));
     acc = warp_reduce<A>(acc);
     if (lane == 0) {
       if (a.has_seed) acc = A::comb(A::lift(from_bits<T>(a.seed)), acc);
@@ -164,6 +176,7 @@ struct SplitArgs {
   uint32_t *tickets;  // outer counters, zero between launches
   uint64_t seed;
   int has_seed;
+  uint64_t mapc;      // the constant of a fused map (bits of one element)
 };
 
 template <int OP, class T, int PREC, int ZOP = NO_ZIP>
@@ -176,8 +189,9 @@ __global__ void __launch_bounds__(256) fold_split(SplitArgs a) {
   for (int64_t job = blockIdx.x; job < a.outer * G; job += gridDim.x) {
     const int64_t r = job / G, g = job % G;
     const T *p = static_cast<const T *>(a.in) + r * a.inner;
-    const T *q = ZOP == NO_ZIP ? nullptr : static_cast<const T *>(a.in2) + r * a.inner;
-    S acc = reduce_span<A, T, ZOP>(p, a.inner, g * blockDim.x + threadIdx.x, G * blockDim.x, q);
+    const T *q = zips<ZOP>() ? static_cast<const T *>(a.in2) + r * a.inner : nullptr;
+    S acc = reduce_span<A, T, ZOP>(p, a.inner, g * blockDim.x + threadIdx.x, G * blockDim.x, q,
+                                   from_bits<T>(a.mapc));
     acc = block_reduce<A>(acc);
     if (threadIdx.x == 0) {
       parts[r * G + g] = acc;
@@ -209,10 +223,10 @@ __global__ void __launch_bounds__(256) fold_split(SplitArgs a) {
 // ----------------------------------------------------------------- host side
 template <int OP, class T, int PREC, int ZOP = NO_ZIP>
 int fold_typed(Workspace *w, const T *in, T *out, int64_t outer, int64_t inner, bool has_seed,
-               uint64_t seed, cudaStream_t s, const T *in2 = nullptr) {
+               uint64_t seed, cudaStream_t s, const T *in2 = nullptr, uint64_t mapc = 0) {
   using S = typename Acc<OP, T, PREC>::S;
   const Device &d = device_info();
-  FoldArgs fa{in, out, in2, outer, inner, seed, has_seed};
+  FoldArgs fa{in, out, in2, outer, inner, seed, has_seed, mapc};
   if (inner <= 16) {
     int64_t blocks = cdiv_h(outer, 256);
     if (blocks > (int64_t)d.sms * 16) blocks = (int64_t)d.sms * 16;
@@ -230,7 +244,7 @@ int fold_typed(Workspace *w, const T *in, T *out, int64_t outer, int64_t inner, 
   }
   // Split each row over G CTAs: aim at ~4 resident CTAs of 256 threads per SM
   // over the whole grid, each thread with at least 4 vectors to stream.
-  const int64_t vec_per_row = cdiv_h(row_bytes * (ZOP == NO_ZIP ? 1 : 2), 16);
+  const int64_t vec_per_row = cdiv_h(row_bytes * (zips<ZOP>() ? 2 : 1), 16);
   int64_t G = cdiv_h((int64_t)d.sms * 4, outer);
   const int64_t gmax = cdiv_h(vec_per_row, 256 * 4);
   if (G > gmax) G = gmax;
@@ -240,7 +254,7 @@ int fold_typed(Workspace *w, const T *in, T *out, int64_t outer, int64_t inner, 
   if (st) return st;
   st = ws_scratch(w, (size_t)jobs * sizeof(S));
   if (st) return st;
-  SplitArgs sa{in, out, in2, outer, inner, G, w->scratch, w->words + W_ROWTICKET0, seed, has_seed};
+  SplitArgs sa{in, out, in2, outer, inner, G, w->scratch, w->words + W_ROWTICKET0, seed, has_seed, mapc};
   int64_t blocks = jobs;
   if (blocks > (int64_t)d.sms * 8) blocks = (int64_t)d.sms * 8;
   fold_split<OP, T, PREC, ZOP><<<(unsigned)blocks, 256, 0, s>>>(sa);

@@ -434,11 +434,13 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
   // One warp waits for the tile; the others block at the CTA barrier, which
   // costs no issue slots (several CTAs share an SM and the walk is
   // issue-bound).  The barrier orders every thread after the completed load.
+  bool landed = true;
   if (warp == 0 && !mbar_wait_sleep(&bar, 0)) {
     if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
-    mbar_wait_sleep(&bar, 0);
+    landed = mbar_wait_sleep(&bar, 0);
   }
-  __syncthreads();
+  // A tile whose load never landed is neither read nor published.
+  if (__syncthreads_or(!landed)) return;
   const bool ok = s_bad == 0;
   if (!ok && tid == 0) raise_error(a.err, DEV_ERR_INDEX);
   const int lo = (int)s_lo, hi = (int)s_hi;
@@ -616,6 +618,7 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
       int64_t k0 = 0;
       bool gave_up = false;
       uint32_t it = 0;
+      uint64_t t_wait = 0;
       while (true) {
         uint32_t fl[LB];
         S v[LB];
@@ -640,8 +643,10 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
           kp = lb_window<LB>(fl, resolved, whole);
           if (resolved || whole) break;
           ++it;
+          if (it == 1) t_wait = global_ns();
           const bool stop = gave_up || it > SPIN_LIMIT ||
-                            ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
+                            ((it & 63u) == 0 && ((ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u ||
+                                                 global_ns() - t_wait > WAIT_LIMIT_NS));
           if (__any_sync(0xffffffffu, stop)) {
             gave_up = true;
             if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);

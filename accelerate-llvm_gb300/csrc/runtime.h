@@ -11,6 +11,8 @@
 #include <cstddef>
 #include <cstring>
 #include <atomic>
+#include <iterator>
+#include <map>
 #include <mutex>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -43,7 +45,7 @@ enum : uint32_t {
   DEV_ERR_INDEX   = 2u,  // permute target index out of range
 };
 
-enum { W_ERR = 0, W_TICKET = 1, W_SEGBIG = 2, W_ROWTICKET0 = 8 };
+enum { W_ERR = 0, W_TICKET = 1, W_SEGBIG = 2, W_DONE = 3, W_ROWTICKET0 = 8 };
 
 struct Device {
   int id;
@@ -157,5 +159,56 @@ template <class T> inline uint64_t seed_bits(const void *seed) {
 }
 
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Best-fit allocation of ranges of one arena (offsets and sizes in bytes,
+// the caller rounds sizes to its alignment); freed ranges coalesce with free
+// neighbours.  Host-side bookkeeping only: the arena itself is one device
+// allocation made by its owner (a memory table, the serving loop).
+struct RangeAlloc {
+  std::map<int64_t, int64_t> free_off;        // offset -> size
+  std::multimap<int64_t, int64_t> free_size;  // size -> offset
+  int64_t free_bytes = 0;
+
+  void give(int64_t off, int64_t size) {
+    free_bytes += size;
+    auto erase_size = [&](int64_t o, int64_t sz) {
+      auto r = free_size.equal_range(sz);
+      for (auto it = r.first; it != r.second; ++it)
+        if (it->second == o) { free_size.erase(it); return; }
+    };
+    auto next = free_off.lower_bound(off);
+    if (next != free_off.end() && next->first == off + size) {
+      size += next->second;
+      erase_size(next->first, next->second);
+      next = free_off.erase(next);
+    }
+    if (next != free_off.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        off = prev->first;
+        size += prev->second;
+        erase_size(prev->first, prev->second);
+        free_off.erase(prev);
+      }
+    }
+    free_off[off] = size;
+    free_size.emplace(size, off);
+  }
+
+  bool take(int64_t size, int64_t *off) {
+    auto it = free_size.lower_bound(size);
+    if (it == free_size.end()) return false;
+    const int64_t sz = it->first, o = it->second;
+    free_size.erase(it);
+    free_off.erase(o);
+    if (sz > size) {
+      free_off[o + size] = sz - size;
+      free_size.emplace(sz - size, o + size);
+    }
+    free_bytes -= size;
+    *off = o;
+    return true;
+  }
+};
 
 }  // namespace accgb

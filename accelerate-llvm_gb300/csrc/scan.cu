@@ -230,3 +230,16 @@ extern "C" int acc_scan_noalloc(int op, int type, int prec, int dir, int kind, c
     });
   });
 }
+
+extern "C" int acc_scan_noalloc_status(void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_status(e);
+  NoallocDevice *nd = nullptr;
+  int st = noalloc_setup(&nd);
+  if (st) return st;
+  uint32_t err = 0;
+  e = cudaMemcpy(&err, nd->ptr->words + 0, sizeof(err), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e);
+  return (err & DEV_ERR_TIMEOUT) ? ACC_ERR_TIMEOUT : ACC_OK;
+}

@@ -57,13 +57,15 @@ struct ScanArgs {
   uint64_t *status;
   uint32_t *ticket;
   uint32_t *err;
+  uint32_t *done;    // persistent kernels: CTAs finished (the last re-arms the ticket)
   uint32_t epoch;
   int has_seed;
   int exclusive;
   int tma_in;
   int tma_out;
   const void *in2;   // ZIP kernels: the scanned element i is zop(in[i], in2[i])
-  int zop;
+  int zop;           // ... MAP kernels: it is zop(in[i], c)
+  uint64_t mapc;     // MAP kernels: the constant c (bits of one element)
 };
 
 __device__ __forceinline__ int swz(int row, int chunk) { return row * SCAN_ROW_BYTES + ((chunk ^ (row & 7)) << 4); }
@@ -96,6 +98,93 @@ __device__ __forceinline__ uint32_t decode(SlotWords s, uint32_t epoch, S &v) {
   return tag & 3u;
 }
 
+// Warp-collective decoupled look-back of a tile that is not the first one:
+// the combination of every predecessor's value, walking from the nearest
+// predecessor outwards in windows of 32 * LB tiles (LB consecutive slots per
+// lane, all of a poll's loads issued back to back) up to the nearest
+// published inclusive prefix.  Every lane returns the result.  A window that
+// is not resolved after WAIT_LIMIT_NS (or SPIN_LIMIT polls, or once another
+// CTA has timed out) gives up: its missing slots count as the identity and
+// the error word records DEV_ERR_TIMEOUT.
+template <class A, bool R2L, int LB>
+__device__ __forceinline__ typename A::S lookback_prefix(const ScanArgs &a, int64_t tile) {
+  using S = typename A::S;
+  const int lane = threadIdx.x & 31;
+  S acc = A::id();
+  int64_t k0 = 0;
+  bool gave_up = false;
+  while (true) {
+    uint32_t fl[LB];
+    S v[LB];
+    bool ex[LB];
+#pragma unroll
+    for (int i = 0; i < LB; ++i) {
+      const int64_t d = k0 + lane * LB + i;  // 0 = nearest predecessor
+      const int64_t pt = R2L ? tile + 1 + d : tile - 1 - d;
+      ex[i] = R2L ? (pt < a.ntiles) : (pt >= 0);
+      fl[i] = ex[i] ? 0u : 2u;
+      v[i] = A::id();
+    }
+    uint32_t it = 0;
+    uint64_t t_wait = 0;
+    bool resolved = false, whole = false;
+    int kp = 32;
+    while (true) {
+      // Issue every pending slot load of this poll first, then decode:
+      // one round trip per poll, not one per slot.  Lanes beyond the
+      // nearest inclusive prefix seen so far need no more reads.
+      const int kp0 = lb_stop_lane<LB>(fl);
+      SlotWords sw[LB];
+#pragma unroll
+      for (int i = 0; i < LB; ++i) {
+        sw[i] = SlotWords{0ull, 0ull};
+        if (ex[i] && fl[i] == 0 && lane <= kp0) {
+          const int64_t d = k0 + lane * LB + i;
+          sw[i] = ld_slot(a.status + 2 * (R2L ? tile + 1 + d : tile - 1 - d));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < LB; ++i)
+        if (ex[i] && fl[i] == 0 && lane <= kp0) fl[i] = decode<S>(sw[i], a.epoch, v[i]);
+      kp = lb_window<LB>(fl, resolved, whole);
+      if (resolved || whole) break;
+      ++it;
+      // Give up (warp-uniformly) after WAIT_LIMIT_NS or SPIN_LIMIT polls, or
+      // at once when another CTA on this stream has already timed out.
+      if (it == 1) t_wait = global_ns();
+      const bool stop = gave_up || it > SPIN_LIMIT ||
+                        ((it & 63u) == 0 && ((ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u ||
+                                             global_ns() - t_wait > WAIT_LIMIT_NS));
+      if (__any_sync(0xffffffffu, stop)) {
+        gave_up = true;
+        if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
+#pragma unroll
+        for (int i = 0; i < LB; ++i)
+          if (fl[i] == 0) fl[i] = 2u;  // treat as identity: the result is flagged as failed
+        kp = lb_window<LB>(fl, resolved, whole);
+        break;
+      }
+      __nanosleep(it < 8 ? 32 : 128);
+    }
+    // Lane-local fold from the nearest predecessor outwards, up to and
+    // including the first inclusive prefix.
+    bool seen_p = false;
+    S lv = A::id();
+#pragma unroll
+    for (int i = 0; i < LB; ++i) {
+      if (!seen_p) lv = R2L ? A::comb(lv, v[i]) : A::comb(v[i], lv);
+      seen_p = seen_p || fl[i] == 2u;
+    }
+    if (lane > kp) lv = A::id();
+    S wv = R2L ? warp_reduce<A>(lv) : warp_reduce_rev<A>(lv);
+    wv = shfl_idx(wv, 0);
+    acc = R2L ? A::comb(acc, wv) : A::comb(wv, acc);
+    if (resolved) break;
+    k0 += 32 * LB;
+  }
+  return acc;
+}
+
 // One tile = SUB sub-tiles of 256 rows x 128 B; thread t owns row t of every
 // sub-tile.  The rows of the array's full 128 B lines are in `buf` (each
 // sub-tile 32 KiB, 128-byte swizzled); the last, partial line is read from
@@ -111,8 +200,10 @@ struct NoSubDone {
 };
 
 // With ZIP, the rows read from global memory are zipped as they are read
-// (the rows in `buf` arrive zipped).
-template <int OP, class T, int PREC, bool R2L, int SUB, bool ZIP = false, class SubDone = NoSubDone>
+// (the rows in `buf` arrive zipped).  With MAP, every element is mapped as it
+// is read, from `buf` or from global memory (map (\x -> zop x c)).
+template <int OP, class T, int PREC, bool R2L, int SUB, bool ZIP = false, bool MAP = false,
+          class SubDone = NoSubDone>
 __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile, const ScanArgs &a,
                                                typename Acc<OP, T, PREC>::S (*s_warp)[SCAN_THREADS / 32],
                                                typename Acc<OP, T, PREC>::S &s_prefix, bool smem_all_rows,
@@ -135,6 +226,11 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
         uint4 v = *reinterpret_cast<const uint4 *>(buf + u * SUB_BYTES + swz(tid, c));
         memcpy(&x[c * VEC], &v, 16);
       }
+      if constexpr (MAP) {
+        const T cm = from_bits<T>(a.mapc);
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) x[j] = zip_elem(a.zop, x[j], cm);
+      }
     } else {
       const T *src = static_cast<const T *>(a.in);
       const int64_t e0 = grow * ITEMS;
@@ -142,6 +238,10 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
         const T *src2 = static_cast<const T *>(a.in2);
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? zip_elem(a.zop, src[e0 + j], src2[e0 + j]) : idT;
+      } else if constexpr (MAP) {
+        const T cm = from_bits<T>(a.mapc);
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? zip_elem(a.zop, src[e0 + j], cm) : idT;
       } else {
 #pragma unroll
         for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
@@ -187,79 +287,7 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
       prefix = a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id();
     } else {
       if (lane == 0) publish<S>(a.status, tile, a.epoch, 1u, bagg);
-      // Each lane inspects LB consecutive predecessors per round trip, so one
-      // window covers 32 * LB tiles.
-      constexpr int LB = SCAN_LOOKBACK;
-      S acc = A::id();
-      int64_t k0 = 0;
-      bool gave_up = false;
-      while (true) {
-        uint32_t fl[LB];
-        S v[LB];
-        bool ex[LB];
-#pragma unroll
-        for (int i = 0; i < LB; ++i) {
-          const int64_t d = k0 + lane * LB + i;  // 0 = nearest predecessor
-          const int64_t pt = R2L ? tile + 1 + d : tile - 1 - d;
-          ex[i] = R2L ? (pt < a.ntiles) : (pt >= 0);
-          fl[i] = ex[i] ? 0u : 2u;
-          v[i] = A::id();
-        }
-        uint32_t it = 0;
-        bool resolved = false, whole = false;
-        int kp = 32;
-        while (true) {
-          // Issue every pending slot load of this poll first, then decode:
-          // one round trip per poll, not one per slot.  Lanes beyond the
-          // nearest inclusive prefix seen so far need no more reads.
-          const int kp0 = lb_stop_lane<LB>(fl);
-          SlotWords sw[LB];
-#pragma unroll
-          for (int i = 0; i < LB; ++i) {
-            sw[i] = SlotWords{0ull, 0ull};
-            if (ex[i] && fl[i] == 0 && lane <= kp0) {
-              const int64_t d = k0 + lane * LB + i;
-              sw[i] = ld_slot(a.status + 2 * (R2L ? tile + 1 + d : tile - 1 - d));
-            }
-          }
-#pragma unroll
-          for (int i = 0; i < LB; ++i)
-            if (ex[i] && fl[i] == 0 && lane <= kp0) fl[i] = decode<S>(sw[i], a.epoch, v[i]);
-          kp = lb_window<LB>(fl, resolved, whole);
-          if (resolved || whole) break;
-          ++it;
-          // Give up (warp-uniformly) after SPIN_LIMIT polls, or at once when
-          // another CTA on this stream has already timed out.
-          const bool stop = gave_up || it > SPIN_LIMIT ||
-                            ((it & 63u) == 0 && (ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u);
-          if (__any_sync(0xffffffffu, stop)) {
-            gave_up = true;
-            if (lane == 0) raise_error(a.err, DEV_ERR_TIMEOUT);
-#pragma unroll
-            for (int i = 0; i < LB; ++i)
-              if (fl[i] == 0) fl[i] = 2u;  // treat as identity: the result is flagged as failed
-            kp = lb_window<LB>(fl, resolved, whole);
-            break;
-          }
-          __nanosleep(it < 8 ? 32 : 128);
-        }
-        // Lane-local fold from the nearest predecessor outwards, up to and
-        // including the first inclusive prefix.
-        bool seen_p = false;
-        S lv = A::id();
-#pragma unroll
-        for (int i = 0; i < LB; ++i) {
-          if (!seen_p) lv = R2L ? A::comb(lv, v[i]) : A::comb(v[i], lv);
-          seen_p = seen_p || fl[i] == 2u;
-        }
-        if (lane > kp) lv = A::id();
-        S wv = R2L ? warp_reduce<A>(lv) : warp_reduce_rev<A>(lv);
-        wv = shfl_idx(wv, 0);
-        acc = R2L ? A::comb(acc, wv) : A::comb(wv, acc);
-        if (resolved) break;
-        k0 += 32 * LB;
-      }
-      prefix = acc;
+      prefix = lookback_prefix<A, R2L, SCAN_LOOKBACK>(a, tile);
     }
     const S inclusive = R2L ? A::comb(bagg, prefix) : A::comb(prefix, bagg);
     if (lane == 0) {
@@ -316,7 +344,7 @@ __device__ __forceinline__ void scan_tile_body(unsigned char *buf, int64_t tile,
 
 // One tile per CTA, any alignment: coalesced loads / stores through the same
 // swizzled smem layout (used when a TMA descriptor cannot describe the array).
-template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false, bool MAP = false>
 __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(ScanArgs a) {
   using S = typename Acc<OP, T, PREC>::S;
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
@@ -347,6 +375,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(ScanArgs a)
     T v = idT;
     if (gi < a.n) {
       if constexpr (ZIP) v = zip_elem(a.zop, src[gi], src2[gi]);
+      else if constexpr (MAP) v = zip_elem(a.zop, src[gi], from_bits<T>(a.mapc));
       else v = src[gi];
     }
     const int r = e / ITEMS, k = e % ITEMS;
@@ -368,7 +397,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_lookback_kernel(ScanArgs a)
 // One tile (SUB x 32 KiB) per CTA through TMA, for 16-byte aligned arrays:
 // the tile arrives with SUB 2-D TMA loads of [256 rows x 128 B] on one
 // mbarrier, is scanned in shared memory, and leaves with SUB TMA stores.
-template <int OP, class T, int PREC, bool R2L, int SUB>
+template <int OP, class T, int PREC, bool R2L, int SUB, bool MAP = false>
 __global__ void __launch_bounds__(SCAN_THREADS, SUB == 1 ? 6 : 3)
 scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
   using S = typename Acc<OP, T, PREC>::S;
@@ -394,10 +423,9 @@ scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__
   }
   __syncthreads();
   const int64_t tile = s_tile;
-  if (!mbar_wait(&bar, 0)) {
-    raise_error(a.err, DEV_ERR_TIMEOUT);
-    mbar_wait(&bar, 0);
-  }
+  // A tile whose load never landed is neither read nor published: its
+  // successors' look-backs give up in turn and the call reports the timeout.
+  if (__syncthreads_or(!mbar_wait_flagged(&bar, 0, a.err))) return;
   // Each sub-tile leaves by TMA as soon as it is rescanned, while the next
   // one is rescanned; the CTA waits only for the last store's reads.
   auto store_sub = [&](int u) {
@@ -408,8 +436,254 @@ scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__
       tma_store_commit();
     }
   };
-  scan_tile_body<OP, T, PREC, R2L, SUB>(buf, tile, a, s_warp, s_prefix, false, store_sub);
+  scan_tile_body<OP, T, PREC, R2L, SUB, false, MAP>(buf, tile, a, s_warp, s_prefix, false, store_sub);
   if (tid == 0) tma_store_wait_read();
+}
+
+// --------------------------------------------------------------------------
+// Persistent single-pass scan with a re-read from L2, for 16-byte aligned
+// 1-D arrays.  A tile (32 KiB: 256 rows x 128 B, thread t owns row t) is
+// read from HBM into buffer A and folded (pass 1: row totals, warp scans, the
+// tile aggregate, published at once); its buffer is then free and takes the
+// CTA's next tile while a look-back warp resolves the tile's exclusive
+// prefix from its predecessors' published values.  Pass 2 loads the tile
+// again into buffer B -- from L2, where pass 1 left it a few microseconds
+// earlier -- rescans it from its prefix and stores it by TMA.  So a tile
+// occupies shared memory only while it is worked on, never while its
+// look-back waits, and the look-back of tile i overlaps the HBM load and fold
+// of tile i+1; DRAM still sees each input byte read once.
+// Roles: 256 compute threads (8 warps) and one look-back warp; they hand
+// tiles over through mbarriers (aggr: the aggregate of the tile in slot p is
+// published; pref: its exclusive prefix is known).  Tiles come from a
+// dynamic ticket, so that each tile's predecessors are always claimed by
+// running CTAs; the grid is launched cooperatively (every CTA resident), and
+// a CTA folds and publishes its next tile before it waits for its current
+// tile's prefix, so the lowest unfinished tile can always finish.  Every
+// wait is bounded: a wait that runs out stops the CTA (after a bounded wait
+// for its copies in flight) and raises DEV_ERR_TIMEOUT.
+constexpr int L2S_COMPUTE = SCAN_THREADS;
+constexpr int L2S_THREADS = L2S_COMPUTE + 32;
+constexpr int L2S_TILE = SCAN_THREADS * SCAN_ROW_BYTES;
+constexpr int L2S_CTAS_PER_SM = 3;
+
+template <int OP, class T, int PREC, bool R2L>
+__global__ void __launch_bounds__(L2S_THREADS, L2S_CTAS_PER_SM)
+scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+  using A = Acc<OP, T, PREC>;
+  using S = typename A::S;
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  constexpr int VEC = 16 / sizeof(T);
+  constexpr int NWARP = L2S_COMPUTE / 32;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *bufA = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char *bufB = bufA + L2S_TILE;
+  __shared__ uint64_t fullA, fullB, aggr[2], pref[2];
+  __shared__ int64_t s_claim;    // dynamic index of the tile pass 1 takes next
+  __shared__ int64_t s_tile[2];  // tile in look-back slot p (-1: stop)
+  __shared__ S s_warp[2][NWARP];
+  __shared__ S s_agg[2], s_prefix[2];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  auto tile_of = [&](int64_t d) { return R2L ? a.ntiles - 1 - d : d; };
+
+  if (tid == 0) {
+    mbar_init(&fullA, 1);
+    mbar_init(&fullB, 1);
+    mbar_init(&aggr[0], 1);
+    mbar_init(&aggr[1], 1);
+    mbar_init(&pref[0], 1);
+    mbar_init(&pref[1], 1);
+    fence_mbar_init();
+    prefetch_tmap(&tin);
+    prefetch_tmap(&tout);
+    const int64_t d = (int64_t)atomicAdd(a.ticket, 1u);
+    s_claim = d;
+    if (d < a.ntiles) {
+      mbar_expect_tx(&fullA, L2S_TILE);
+      tma_load_2d(bufA, &tin, 0, (int)(tile_of(d) * SCAN_THREADS), &fullA);
+    }
+  }
+  __syncthreads();
+
+  if (warp == NWARP) {
+    // ---- look-back warp: the exclusive prefix of each tile, in this CTA's order
+    for (int64_t k = 0;; ++k) {
+      const int p = (int)(k & 1);
+      const bool ok = mbar_wait_flagged(&aggr[p], (uint32_t)(k >> 1) & 1u, a.err);
+      if (__any_sync(0xffffffffu, !ok)) break;
+      const int64_t tile = s_tile[p];
+      if (tile < 0) break;
+      const bool first = R2L ? (tile == a.ntiles - 1) : (tile == 0);
+      const S prefix = first ? (a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id())
+                             : lookback_prefix<A, R2L, SCAN_LOOKBACK>(a, tile);
+      if (lane == 0) {
+        const S bagg = s_agg[p];
+        const S inclusive = R2L ? A::comb(bagg, prefix) : A::comb(prefix, bagg);
+        publish<S>(a.status, tile, a.epoch, 2u, inclusive);
+        s_prefix[p] = prefix;
+        const bool last = R2L ? (tile == 0) : (tile == a.ntiles - 1);
+        if (last && a.total_out) *static_cast<T *>(a.total_out) = A::lower(inclusive);
+        if (first && a.seed_out) *static_cast<T *>(a.seed_out) = from_bits<T>(a.seed);
+        mbar_arrive(&pref[p]);
+      }
+      __syncwarp();
+    }
+    return;
+  }
+
+  // ---- compute warps
+  const T idT = Prim<OP, T>::id();
+  const T *src = static_cast<const T *>(a.in);
+  T *dst = static_cast<T *>(a.out);
+  auto load_row = [&](const unsigned char *buf, int64_t tile, T (&x)[ITEMS]) {
+    const int64_t grow = tile * SCAN_THREADS + tid;
+    if (grow < a.full_rows) {
+#pragma unroll
+      for (int c = 0; c < ITEMS / VEC; ++c) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(tid, c));
+        memcpy(&x[c * VEC], &v, 16);
+      }
+    } else {
+      const int64_t e0 = grow * ITEMS;
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
+    }
+  };
+  int64_t d_new = s_claim;
+  int64_t t_cur = -1;
+  S excl_cur = A::id();
+  int64_t k = 0;  // tiles this CTA has taken
+  uint32_t phA = 0, phB = 0;
+  bool failed = false, b_loading = false;
+  while (true) {
+    const bool have_new = d_new < a.ntiles;
+    const int pn = (int)(k & 1), pc = pn ^ 1;
+    int64_t t_new = -1;
+    S excl_new = A::id();
+    if (have_new) {
+      // pass 1 of the new tile (in A)
+      t_new = tile_of(d_new);
+      if (named_bar_or<1, L2S_COMPUTE>(!mbar_wait_flagged(&fullA, phA, a.err))) { failed = true; break; }
+      phA ^= 1u;
+      T x[ITEMS];
+      load_row(bufA, t_new, x);
+      if (!R2L) {
+        S agg = A::lift(x[0]);
+#pragma unroll
+        for (int j = 1; j < ITEMS; ++j) agg = A::push(agg, x[j]);
+        const S incl = warp_scan_incl<A>(agg);
+        const S up = shfl_up(incl, 1);
+        excl_new = lane == 0 ? A::id() : up;
+        if (lane == 31) s_warp[pn][warp] = incl;
+      } else {
+        S agg = A::lift(x[ITEMS - 1]);
+#pragma unroll
+        for (int j = ITEMS - 2; j >= 0; --j) agg = A::push(agg, x[j]);
+        const S incl = warp_scan_incl_rev<A>(agg);
+        const S dn = shfl_down(incl, 1);
+        excl_new = lane == 31 ? A::id() : dn;
+        if (lane == 0) s_warp[pn][warp] = incl;
+      }
+      named_bar_sync<1, L2S_COMPUTE>();  // A is read; the warp totals are in place
+      if (tid == 0) {
+        S bagg = s_warp[pn][0];
+#pragma unroll
+        for (int w = 1; w < NWARP; ++w) bagg = A::comb(bagg, s_warp[pn][w]);
+        s_agg[pn] = bagg;
+        s_tile[pn] = t_new;
+        const bool first = R2L ? (t_new == a.ntiles - 1) : (t_new == 0);
+        if (!first) publish<S>(a.status, t_new, a.epoch, 1u, bagg);
+        mbar_arrive(&aggr[pn]);
+        // the CTA's next tile: its HBM load runs during this tile's look-back
+        const int64_t dn = (int64_t)atomicAdd(a.ticket, 1u);
+        s_claim = dn;
+        if (dn < a.ntiles) {
+          mbar_expect_tx(&fullA, L2S_TILE);
+          tma_load_2d(bufA, &tin, 0, (int)(tile_of(dn) * SCAN_THREADS), &fullA);
+        }
+      }
+    } else if (tid == 0) {
+      s_tile[pn] = -1;  // no more tiles: the look-back warp stops
+      mbar_arrive(&aggr[pn]);
+    }
+    if (t_cur >= 0) {
+      // pass 2 of the current tile: load it again (from L2) into B, rescan it
+      // from its prefix, store it
+      if (tid == 0) {
+        tma_store_wait_read();  // the previous store has read B
+        mbar_expect_tx(&fullB, L2S_TILE);
+        tma_load_2d(bufB, &tin, 0, (int)(t_cur * SCAN_THREADS), &fullB);
+      }
+      b_loading = true;
+      const bool okp = mbar_wait_flagged(&pref[pc], (uint32_t)((k - 1) >> 1) & 1u, a.err);
+      const bool okb = mbar_wait_flagged(&fullB, phB, a.err);
+      if (named_bar_or<1, L2S_COMPUTE>(!(okp && okb))) { failed = true; break; }
+      phB ^= 1u;
+      b_loading = false;
+      S inner = A::id();
+      if (!R2L) {
+        for (int w = 0; w < warp; ++w) inner = A::comb(inner, s_warp[pc][w]);
+      } else {
+        for (int w = warp + 1; w < NWARP; ++w) inner = A::comb(inner, s_warp[pc][w]);
+      }
+      const S pfx = s_prefix[pc];
+      S run = R2L ? A::comb(A::comb(excl_cur, inner), pfx) : A::comb(pfx, A::comb(inner, excl_cur));
+      T x[ITEMS];
+      load_row(bufB, t_cur, x);
+      const int64_t grow = t_cur * SCAN_THREADS + tid;
+      const bool in_smem = grow < a.full_rows;
+      const int64_t e0 = grow * ITEMS;
+#pragma unroll
+      for (int cc = 0; cc < ITEMS / VEC; ++cc) {
+        const int c = R2L ? ITEMS / VEC - 1 - cc : cc;
+        T y[VEC];
+#pragma unroll
+        for (int kk = 0; kk < VEC; ++kk) {
+          const int q = R2L ? VEC - 1 - kk : kk;
+          const int j = c * VEC + q;
+          if (a.exclusive) { y[q] = A::lower(run); run = A::push(run, x[j]); }
+          else { run = A::push(run, x[j]); y[q] = A::lower(run); }
+        }
+        if (in_smem) {
+          uint4 v;
+          memcpy(&v, y, 16);
+          *reinterpret_cast<uint4 *>(bufB + swz(tid, c)) = v;
+        } else {
+#pragma unroll
+          for (int q = 0; q < VEC; ++q)
+            if (e0 + c * VEC + q < a.n) dst[e0 + c * VEC + q] = y[q];
+        }
+      }
+      fence_proxy_async_smem();
+      named_bar_sync<1, L2S_COMPUTE>();
+      if (tid == 0) {
+        tma_store_2d(&tout, 0, (int)(t_cur * SCAN_THREADS), bufB);
+        tma_store_commit();
+      }
+    }
+    named_bar_sync<1, L2S_COMPUTE>();  // s_claim is in place
+    if (!have_new) break;
+    d_new = s_claim;
+    t_cur = t_new;
+    excl_cur = excl_new;
+    ++k;
+  }
+  if (tid == 0) {
+    if (failed) {
+      raise_error(a.err, DEV_ERR_TIMEOUT);
+      // bounded waits for this CTA's loads still in flight
+      if (s_claim < a.ntiles) mbar_wait(&fullA, phA);
+      if (b_loading) mbar_wait(&fullB, phB);
+      s_tile[(int)(k & 1)] = -1;
+      mbar_arrive(&aggr[(int)(k & 1)]);
+    }
+    tma_store_wait_all();
+    // The last CTA to finish re-arms the ticket for the next launch.
+    __threadfence();
+    if (atomicAdd(a.done, 1u) == gridDim.x - 1) {
+      *a.ticket = 0u;
+      *a.done = 0u;
+    }
+  }
 }
 
 // Zip one thread's 128-byte row of the two swizzled tiles into the first:
@@ -465,10 +739,9 @@ scan_zip_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_consta
   }
   __syncthreads();
   const int64_t tile = s_tile;
-  if (!mbar_wait(&bar, 0)) {
-    raise_error(a.err, DEV_ERR_TIMEOUT);
-    mbar_wait(&bar, 0);
-  }
+  // A tile whose load never landed is neither read nor published: its
+  // successors' look-backs give up in turn and the call reports the timeout.
+  if (__syncthreads_or(!mbar_wait_flagged(&bar, 0, a.err))) return;
   // Rows past the array's full 128 B lines are read (and zipped) from global
   // memory by the tile body.
   if (tile * SCAN_THREADS + tid < a.full_rows) {
@@ -507,10 +780,11 @@ struct RowScanArgs {
   int seed_at_end;   // scanr z: out[row][inner] = z
   int total_at_end;  // scanl z: out[row][inner] = total
   const void *in2;   // ZIP kernels: element e of row r is zop(in[r][e], in2[r][e]) (pitch in_pitch)
-  int zop;
+  int zop;           // ... MAP kernels: it is zop(in[r][e], c)
+  uint64_t mapc;     // MAP kernels: the constant c (bits of one element)
 };
 
-template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false, bool MAP = false>
 __global__ void __launch_bounds__(256) scan_rows_kernel(RowScanArgs a) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
@@ -537,6 +811,7 @@ __global__ void __launch_bounds__(256) scan_rows_kernel(RowScanArgs a) {
         x[j] = idT;
         if (e0 + j < a.inner) {
           if constexpr (ZIP) x[j] = zip_elem(a.zop, src[e0 + j], src2[e0 + j]);
+          else if constexpr (MAP) x[j] = zip_elem(a.zop, src[e0 + j], from_bits<T>(a.mapc));
           else x[j] = src[e0 + j];
         }
       }
@@ -597,9 +872,10 @@ __global__ void __launch_bounds__(256) scan_rows_kernel(RowScanArgs a) {
 // ----------------------------------------------------------------- host side
 constexpr size_t SCAN_SMEM = SCAN_THREADS * SCAN_ROW_BYTES + 1024;
 
-template <int OP, class T, int PREC, bool R2L, int SUB>
+template <int OP, class T, int PREC, bool R2L, int SUB, bool MAP = false>
 int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
-                       bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+                       bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s, int mop = 0,
+                       uint64_t mapc = 0) {
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
   CUtensorMap tin, tout;
   memset(&tin, 0, sizeof(tin));
@@ -627,27 +903,105 @@ int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_
   a.has_seed = has_seed;
   a.exclusive = exclusive;
   a.tma_in = a.tma_out = tma;
+  a.zop = mop;
+  a.mapc = mapc;
   if (tma) {
     const size_t smem = (size_t)SUB * SCAN_THREADS * SCAN_ROW_BYTES + 1024;
-    auto kern = scan_tma_kernel<OP, T, PREC, R2L, SUB>;
+    auto kern = scan_tma_kernel<OP, T, PREC, R2L, SUB, MAP>;
     static std::atomic<uint64_t> attr_done{0};
     smem_attrs_once(kern, (int)smem, attr_done);
     kern<<<(unsigned)ntiles, SCAN_THREADS, smem, s>>>(tin, tout, a);
     return check_launch();
   }
-  auto kern = scan_lookback_kernel<OP, T, PREC, R2L>;
+  auto kern = scan_lookback_kernel<OP, T, PREC, R2L, false, MAP>;
   static std::atomic<uint64_t> attr_done{0};
   smem_attrs_once(kern, (int)SCAN_SMEM, attr_done);
   kern<<<(unsigned)ntiles, SCAN_THREADS, SCAN_SMEM, s>>>(a);
   return check_launch();
 }
 
+// The persistent L2-re-read kernel; *launched false when the array cannot be
+// described by a TMA tensor map or the cooperative grid cannot be placed.
+template <int OP, class T, int PREC, bool R2L>
+int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n, bool has_seed,
+                   bool exclusive, uint64_t seed, cudaStream_t s, bool *launched) {
+  constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
+  *launched = false;
+  CUtensorMap tin, tout;
+  memset(&tin, 0, sizeof(tin));
+  memset(&tout, 0, sizeof(tout));
+  const int64_t full_rows = n / ITEMS;
+  if (full_rows == 0 ||
+      !encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true) ||
+      !encode_2d(&tout, out, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true))
+    return ACC_OK;
+  const int64_t ntiles = cdiv_h(n, (int64_t)SCAN_THREADS * ITEMS);
+  // TMA row coordinates are 32-bit: larger arrays take the other kernels.
+  if (ntiles * SCAN_THREADS >= (1ll << 31)) return ACC_OK;
+  const size_t smem = 2 * (size_t)L2S_TILE + 1024;
+  auto kern = scan_l2_kernel<OP, T, PREC, R2L>;
+  static std::atomic<uint64_t> attr_done{0};
+  smem_attrs_once(kern, (int)smem, attr_done);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L2S_THREADS, smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    return ACC_OK;
+  }
+  int st = ws_status(w, (size_t)ntiles * 2);
+  if (st) return st;
+  ScanArgs a{};
+  a.in = in; a.out = out; a.total_out = total_out; a.seed_out = seed_out;
+  a.n = n;
+  a.full_rows = full_rows;
+  a.ntiles = ntiles;
+  a.seed = seed;
+  a.status = w->status;
+  a.ticket = w->words + W_TICKET;
+  a.done = w->words + W_DONE;
+  a.err = w->words + W_ERR;
+  a.epoch = ws_next_epoch(w, s);
+  a.has_seed = has_seed;
+  a.exclusive = exclusive;
+  a.tma_in = a.tma_out = 1;
+  int64_t grid = (int64_t)device_info().sms * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  // A cooperative launch places every CTA at once (or fails): the tiles a CTA
+  // takes wait on tiles that other CTAs hold, so all of them must run together.
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(L2S_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, tin, tout, a);
+  *launched = true;
+  return cuda_status(e);
+}
+
 // Tile size: 2 sub-tiles (64 KiB, 3 CTAs per SM) by default, the faster of
 // the two on GB300 at 2^25..2^28 elements; ACC_GB300_SCAN_SUB=1 selects 32 KiB
-// tiles (6 CTAs per SM).
-template <int OP, class T, int PREC, bool R2L>
+// tiles (6 CTAs per SM).  A scan over a fused map (MAP: map (\x -> mop x c))
+// always takes the 64 KiB tiles.
+template <int OP, class T, int PREC, bool R2L, bool MAP = false>
 int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
-                   bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s) {
+                   bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s, int mop = 0,
+                   uint64_t mapc = 0) {
+  if constexpr (MAP)
+    return launch_scan_1d_sub<OP, T, PREC, R2L, 2, true>(w, in, out, total_out, seed_out, n, has_seed, exclusive,
+                                                          seed, s, mop, mapc);
+  // Arrays of at least four 32 KiB tiles per SM take the persistent
+  // L2-re-read kernel (ACC_GB300_SCAN_KERNEL=tile keeps the tile kernel).
+  static const bool l2k = !(getenv("ACC_GB300_SCAN_KERNEL") && strcmp(getenv("ACC_GB300_SCAN_KERNEL"), "tile") == 0);
+  if (l2k && n * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
+    bool launched = false;
+    const int st = launch_scan_l2<OP, T, PREC, R2L>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s,
+                                                    &launched);
+    if (st || launched) return st;
+  }
   static const int sub = getenv("ACC_GB300_SCAN_SUB") ? atoi(getenv("ACC_GB300_SCAN_SUB")) : 2;
   if (sub == 2)
     return launch_scan_1d_sub<OP, T, PREC, R2L, 2>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
@@ -658,7 +1012,7 @@ int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
 // chunks of 32 elements (one per lane, coalesced), scans each chunk with
 // shuffles and carries the prefix in a register; the semantics are those of
 // scan_rows_kernel (seed placement, exclusive flavours, totals).
-template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false, bool MAP = false>
 __global__ void __launch_bounds__(256) scan_rows_warp_kernel(RowScanArgs a) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
@@ -679,6 +1033,7 @@ __global__ void __launch_bounds__(256) scan_rows_warp_kernel(RowScanArgs a) {
       T x = idT;
       if (e < a.inner) {
         if constexpr (ZIP) x = zip_elem(a.zop, src[e], src2[e]);
+        else if constexpr (MAP) x = zip_elem(a.zop, src[e], from_bits<T>(a.mapc));
         else x = src[e];
       }
       const S v = A::lift(x);
@@ -709,19 +1064,19 @@ __global__ void __launch_bounds__(256) scan_rows_warp_kernel(RowScanArgs a) {
   }
 }
 
-template <int OP, class T, int PREC, bool R2L, bool ZIP = false>
+template <int OP, class T, int PREC, bool R2L, bool ZIP = false, bool MAP = false>
 int launch_scan_rows(const RowScanArgs &a, cudaStream_t s) {
   const Device &d = device_info();
   if (a.inner <= 512 && a.outer >= (int64_t)d.sms * 64) {
     // a warp per row: 8 rows per CTA
     int64_t blocks = cdiv_h(a.outer, 8);
     if (blocks > (int64_t)d.sms * 16) blocks = (int64_t)d.sms * 16;
-    scan_rows_warp_kernel<OP, T, PREC, R2L, ZIP><<<(unsigned)blocks, 256, 0, s>>>(a);
+    scan_rows_warp_kernel<OP, T, PREC, R2L, ZIP, MAP><<<(unsigned)blocks, 256, 0, s>>>(a);
     return check_launch();
   }
   int64_t blocks = a.outer;
   if (blocks > (int64_t)d.sms * 8) blocks = (int64_t)d.sms * 8;
-  scan_rows_kernel<OP, T, PREC, R2L, ZIP><<<(unsigned)blocks, 256, 0, s>>>(a);
+  scan_rows_kernel<OP, T, PREC, R2L, ZIP, MAP><<<(unsigned)blocks, 256, 0, s>>>(a);
   return check_launch();
 }
 
@@ -775,10 +1130,12 @@ int launch_scan_zip_1d(Workspace *w, const T *in, const T *in2, int zop, T *out,
 }
 
 // Every scan flavour over one array, or (ZIP) over zipWith g in in2 with
-// g = zop, both [outer x inner].
-template <int OP, class T, int PREC, bool ZIP = false>
+// g = zop, both [outer x inner], or (MAP) over map (\x -> g x c) in with
+// g = zop and c given by its bits `mapc`.
+template <int OP, class T, int PREC, bool ZIP = false, bool MAP = false>
 int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, int64_t outer,
-               int64_t inner, uint64_t seed, cudaStream_t s, const T *in2 = nullptr, int zop = 0) {
+               int64_t inner, uint64_t seed, cudaStream_t s, const T *in2 = nullptr, int zop = 0,
+               uint64_t mapc = 0) {
   const bool r2l = dir == ACC_R2L;
   const bool seeded = kind != ACC_SCAN_INCLUSIVE;
   // Empty innermost extent: scanl/scanr z give [z]; scanl'/scanr' give
@@ -806,9 +1163,11 @@ int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, in
                                                     exclusive, seed, s);
     } else {
       (void)in2;
-      (void)zop;
-      if (r2l) return launch_scan_1d<OP, T, PREC, true>(w, in, out, total_out, seed_out, inner, seeded, exclusive, seed, s);
-      return launch_scan_1d<OP, T, PREC, false>(w, in, out, total_out, seed_out, inner, seeded, exclusive, seed, s);
+      if (r2l)
+        return launch_scan_1d<OP, T, PREC, true, MAP>(w, in, out, total_out, seed_out, inner, seeded, exclusive,
+                                                      seed, s, zop, mapc);
+      return launch_scan_1d<OP, T, PREC, false, MAP>(w, in, out, total_out, seed_out, inner, seeded, exclusive,
+                                                     seed, s, zop, mapc);
     }
   }
   RowScanArgs a{};
@@ -819,9 +1178,9 @@ int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, in
   a.seed = seed; a.has_seed = seeded; a.exclusive = exclusive;
   a.seed_at_end = kind == ACC_SCAN_SEEDED && r2l;
   a.total_at_end = kind == ACC_SCAN_SEEDED && !r2l;
-  a.in2 = in2; a.zop = zop;
-  if (r2l) return launch_scan_rows<OP, T, PREC, true, ZIP>(a, s);
-  return launch_scan_rows<OP, T, PREC, false, ZIP>(a, s);
+  a.in2 = in2; a.zop = zop; a.mapc = mapc;
+  if (r2l) return launch_scan_rows<OP, T, PREC, true, ZIP, MAP>(a, s);
+  return launch_scan_rows<OP, T, PREC, false, ZIP, MAP>(a, s);
 }
 
 }  // namespace accgb

@@ -1,5 +1,6 @@
 // scan_zip.cu -- scans over a fused producer: scanl / scanl1 / scanr /
-// scanr1 / scanl' / scanr' f z (zipWith g xs ys).
+// scanr1 / scanl' / scanr' f z (zipWith g xs ys), and the same over
+// map (\x -> g x c) xs for a constant c.
 //
 // The reference's scan kernels read a delayed input array: the producer of
 // the scan (here \i -> g (xs!i) (ys!i)) is evaluated inside the scan's first
@@ -67,6 +68,39 @@ extern "C" int acc_scan_zipwith(int op, int zop, int type, int prec, int dir, in
         return scan_typed<OP, T, P, true>(w, dir, kind, static_cast<const T *>(xs), static_cast<T *>(out),
                                           static_cast<T *>(sums), outer, inner, sb, s, static_cast<const T *>(ys),
                                           zop);
+      });
+    });
+  });
+}
+
+extern "C" int acc_scan_map(int op, int gop, int type, int prec, int dir, int kind, const void *xs, const void *c,
+                            void *out, void *sums, int64_t outer, int64_t inner, const void *seed, void *stream) {
+  if (outer < 0 || inner < 0) return ACC_ERR_INVALID;
+  if (op < ACC_ADD || op > ACC_XOR || gop < ACC_ADD || gop > ACC_XOR) return ACC_ERR_INVALID;
+  if (dir != ACC_L2R && dir != ACC_R2L) return ACC_ERR_INVALID;
+  if (kind < ACC_SCAN_INCLUSIVE || kind > ACC_SCAN_PRIME) return ACC_ERR_INVALID;
+  if (kind != ACC_SCAN_INCLUSIVE && !seed) return ACC_ERR_INVALID;
+  if (!c) return ACC_ERR_INVALID;
+  if (outer == 0) return ACC_OK;
+  if (!out && !(inner == 0 && kind != ACC_SCAN_SEEDED)) return ACC_ERR_INVALID;
+  if (inner > 0 && !xs) return ACC_ERR_INVALID;
+  if (kind == ACC_SCAN_PRIME && !sums) return ACC_ERR_INVALID;
+  if (gop != ACC_ADD && gop != ACC_MUL && gop != ACC_MIN && gop != ACC_MAX) return ACC_ERR_UNSUPPORTED;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = ACC_OK;
+  Workspace *w = workspace(s, &st);
+  if (!w) return st;
+  std::lock_guard<std::mutex> lk(w->mu);
+  return with_zip_type(type, [&](auto tv) -> int {
+    using T = decltype(tv);
+    const uint64_t sb = seed_bits<T>(seed);
+    const uint64_t cb = seed_bits<T>(c);
+    return with_scan_op(op, [&](auto opc) -> int {
+      constexpr int OP = decltype(opc)::value;
+      return with_prec<OP, T>(prec, [&](auto pc) -> int {
+        constexpr int P = decltype(pc)::value;
+        return scan_typed<OP, T, P, false, true>(w, dir, kind, static_cast<const T *>(xs), static_cast<T *>(out),
+                                                 static_cast<T *>(sums), outer, inner, sb, s, nullptr, gop, cb);
       });
     });
   });

@@ -7,16 +7,24 @@
 //     queue; each free slot takes either ALL ready small fold / scanl1
 //     requests that fit (packed into one persistent batched launch from the
 //     slot's preallocated batch arena) or the next other request (foldSeg,
-//     permute, stencil, large fold / scan) as a single call.  A request is
-//     admitted only while the bytes held by in-flight requests stay within
-//     the device-memory budget.  Slots free up as their completion events
-//     fire, so new arrivals join while earlier work is still on the GPU.
+//     permute, stencil, large fold / scan) as a single call.  Slots free up
+//     as their completion events fire, so new arrivals join while earlier
+//     work is still on the GPU.
 //   mode 1, plain per-call: every request is launched on its own, in arrival
 //     order, on one stream (the reference's execution model, one launch per
 //     skeleton, PTX/Execute.hs:835-881).
-// Latency = the host time at which the request's completion event is seen
-// minus its arrival time.  Nothing is allocated per request: arenas, events
-// and streams are made before the clock starts.
+// Admission by device memory, in both modes: a request without an output
+// buffer (out == NULL) gets its result space from one device arena of
+// `budget_bytes`, allocated before the clock starts, and is admitted only once
+// that space is free (best fit; the range returns when the request
+// completes); a request with its own output buffer is admitted while the
+// bytes of input and output held by such requests stay within the budget.
+// A request with a host buffer (host_out) has its result copied back to it
+// before it counts as complete.  Latency = the host time at which the
+// request's completion event is seen minus its arrival time.  Nothing is
+// allocated per request: arenas, events and streams are made before the
+// clock starts.
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <deque>
@@ -34,6 +42,19 @@ constexpr int64_t ARENA_REQS = 1024;
 constexpr int64_t ARENA_ITEMS = 1 << 17;
 
 int64_t esize(int type) { return (type == ACC_I64 || type == ACC_F64) ? 8 : 4; }
+
+constexpr int64_t SERVE_ALIGN = 256;
+
+// Bytes of a request's result.
+int64_t out_bytes(const acc_serve_req &q) {
+  switch (q.skeleton) {
+    case ACC_SK_FOLD: return esize(q.type);
+    case ACC_SK_SCAN: return q.n * esize(q.type);
+    case ACC_SK_FOLDSEG: return q.m * esize(q.type);
+    case ACC_SK_PERMUTE: return q.m * 4;
+    default: return q.n * q.m * esize(q.type);
+  }
+}
 
 int64_t held_bytes(const acc_serve_req &q) {
   const int64_t e = esize(q.type);
@@ -95,7 +116,6 @@ struct Slot {
   cudaEvent_t done = nullptr;
   BatchArena *arena = nullptr;
   std::vector<int64_t> ids;
-  int64_t bytes = 0;
   bool busy = false;
 };
 
@@ -123,10 +143,14 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
                          : q.skeleton == ACC_SK_SCAN    ? q.n
                          : q.skeleton == ACC_SK_STENCIL ? q.n * q.m
                                                         : q.m;
-    if ((nin > 0 && !q.in) || (nout > 0 && !q.out) || (q.skeleton == ACC_SK_FOLDSEG && q.m > 0 && !q.aux))
-      return ACC_ERR_INVALID;
+    (void)nout;
+    if ((nin > 0 && !q.in) || (q.skeleton == ACC_SK_FOLDSEG && q.m > 0 && !q.aux)) return ACC_ERR_INVALID;
     if (i > 0 && q.arrival < reqs[i - 1].arrival) return ACC_ERR_INVALID;  // arrival order
-    if (held_bytes(q) > budget_bytes) return ACC_ERR_TOO_LARGE;
+    // A result placed in the arena takes its size rounded up to SERVE_ALIGN
+    // out of an arena of the budget rounded down to SERVE_ALIGN.
+    const int64_t placed_bytes = (out_bytes(q) + SERVE_ALIGN - 1) / SERVE_ALIGN * SERVE_ALIGN;
+    if (q.out ? held_bytes(q) > budget_bytes : placed_bytes > budget_bytes / SERVE_ALIGN * SERVE_ALIGN)
+      return ACC_ERR_TOO_LARGE;
     latency[i] = -1.0;
   }
   if (mode == 1) slots = 1;
@@ -134,6 +158,61 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
   // streams are independent of those, so wait for the device to finish them.
   cudaError_t e0 = cudaDeviceSynchronize();
   if (e0 != cudaSuccess) return cuda_status(e0);
+  // The result arena (only if some request leaves its output to the loop).
+  unsigned char *arena = nullptr;
+  RangeAlloc ranges;
+  bool need_arena = false;
+  for (int64_t i = 0; i < count; ++i) need_arena = need_arena || !reqs[i].out;
+  if (need_arena) {
+    const int64_t cap = budget_bytes / SERVE_ALIGN * SERVE_ALIGN;
+    e0 = cudaMalloc(&arena, (size_t)cap);
+    if (e0 != cudaSuccess) return cuda_status(e0);
+    ranges.give(0, cap);
+  }
+  std::vector<int64_t> out_off(count, -1);
+  int64_t used = 0, arena_used = 0, peak = 0;
+  auto rounded = [](int64_t b) { return (b + SERVE_ALIGN - 1) / SERVE_ALIGN * SERVE_ALIGN; };
+  // Take what request id holds while it is on the GPU; false: not now.
+  auto admit = [&](int64_t id) -> bool {
+    const acc_serve_req &q = reqs[id];
+    if (q.out) {
+      const int64_t hb = held_bytes(q);
+      if (used + hb > budget_bytes) return false;
+      used += hb;
+    } else {
+      const int64_t b = rounded(out_bytes(q));
+      int64_t off = 0;
+      if (b > 0 && !ranges.take(b, &off)) return false;
+      out_off[id] = off;
+      arena_used += b;
+    }
+    if (used + arena_used > peak) peak = used + arena_used;
+    return true;
+  };
+  auto release = [&](int64_t id) {
+    const acc_serve_req &q = reqs[id];
+    if (q.out) {
+      used -= held_bytes(q);
+    } else if (out_off[id] >= 0) {
+      const int64_t b = rounded(out_bytes(q));
+      if (b > 0) ranges.give(out_off[id], b);
+      arena_used -= b;
+      out_off[id] = -1;
+    }
+  };
+  // The request as launched: its own output, or its range of the arena.
+  auto placed = [&](int64_t id) {
+    acc_serve_req q = reqs[id];
+    if (!q.out) q.out = arena + out_off[id];
+    return q;
+  };
+  // Launch request id alone on stream s (its result copied back if asked).
+  auto launch_one = [&](int64_t id, cudaStream_t s) -> int {
+    const acc_serve_req q = placed(id);
+    int r = run_single(q, s);
+    if (r == ACC_OK && q.host_out) r = acc_download(q.host_out, q.out, out_bytes(q), s);
+    return r;
+  };
   std::vector<Slot> sl(slots);
   int st = ACC_OK;
   for (auto &s : sl) {
@@ -151,18 +230,32 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
     }
   // Warm every path once (first launches load modules and size workspaces).
   if (st == ACC_OK) {
-    for (int64_t i = 0; i < count && i < 64 && st == ACC_OK; ++i) st = run_single(reqs[i], sl[0].stream);
-    for (int64_t i = 0; i < count && mode == 0 && st == ACC_OK; ++i)
-      if (batchable(reqs[i])) {
-        const acc_request br = as_batch_request(reqs[i]);
-        for (auto &s : sl)
-          if (st == ACC_OK) st = arena_launch(s.arena, &br, 1, s.stream);
-        break;
+    // Each request is admitted at most once here (its result range is taken
+    // once and given back once, after the device is done with it).
+    std::vector<int64_t> warm;
+    for (int64_t i = 0; i < count && i < 64 && st == ACC_OK; ++i) {
+      if (!admit(i)) continue;
+      warm.push_back(i);
+      st = run_single(placed(i), sl[0].stream);
+    }
+    for (int64_t i = 0; i < count && mode == 0 && st == ACC_OK; ++i) {
+      if (!batchable(reqs[i])) continue;
+      const bool held = i < 64 && std::find(warm.begin(), warm.end(), i) != warm.end();
+      if (!held) {
+        if (!admit(i)) continue;
+        warm.push_back(i);
       }
+      const acc_request br = as_batch_request(placed(i));
+      for (auto &s : sl)
+        if (st == ACC_OK) st = arena_launch(s.arena, &br, 1, s.stream);
+      break;
+    }
     for (auto &s : sl) cudaStreamSynchronize(s.stream);
+    for (int64_t id : warm) release(id);
+    peak = 0;
     if (st == ACC_OK) st = acc_sync(sl[0].stream);
   }
-  int64_t served = 0, batches = 0, max_inflight = 0, inflight = 0, used = 0, peak = 0;
+  int64_t served = 0, batches = 0, max_inflight = 0, inflight = 0;
   const Clock::time_point t0 = Clock::now();
   auto now_s = [&]() { return std::chrono::duration<double>(Clock::now() - t0).count(); };
   if (st == ACC_OK && mode == 0) {
@@ -175,50 +268,57 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
       const double t = now_s();
       while (next < count && reqs[next].arrival <= t) ready.push_back(next++);
       for (auto &s : sl) {
-        if (s.busy && cudaEventQuery(s.done) == cudaSuccess) {
+        if (!s.busy) continue;
+        const cudaError_t q = cudaEventQuery(s.done);
+        if (q != cudaSuccess && q != cudaErrorNotReady) {
+          st = cuda_status(q);  // the device failed: stop serving
+          break;
+        }
+        if (q == cudaSuccess) {
           const double tc = now_s();
-          for (int64_t id : s.ids) latency[id] = tc - reqs[id].arrival;
+          for (int64_t id : s.ids) {
+            latency[id] = tc - reqs[id].arrival;
+            release(id);
+          }
           served += (int64_t)s.ids.size();
           inflight -= (int64_t)s.ids.size();
-          used -= s.bytes;
           s.ids.clear();
-          s.bytes = 0;
           s.busy = false;
           progress = true;
         }
       }
+      if (st != ACC_OK) break;
       for (auto &s : sl) {
         if (s.busy || ready.empty()) continue;
         const acc_serve_req &head = reqs[ready.front()];
         if (batchable(head)) {
-          // Pack every ready small fold / scan that fits the budget and the arena.
+          // Pack every ready small fold / scan that fits the memory budget
+          // and the batch arena.
           pack.clear();
           int64_t items = 0;
           for (auto it = ready.begin(); it != ready.end() && (int64_t)pack.size() < ARENA_REQS;) {
             const acc_serve_req &q = reqs[*it];
-            const int64_t hb = held_bytes(q);
-            if (!batchable(q) || used + hb > budget_bytes) { ++it; continue; }
-            const acc_request br = as_batch_request(q);
-            const int64_t nt = arena_tiles(br);
+            if (!batchable(q)) { ++it; continue; }
+            const int64_t nt = arena_tiles(as_batch_request(q));
             if (items + nt > ARENA_ITEMS) break;
+            if (!admit(*it)) { ++it; continue; }
             items += nt;
-            pack.push_back(br);
+            pack.push_back(as_batch_request(placed(*it)));
             s.ids.push_back(*it);
-            s.bytes += hb;
-            used += hb;
             it = ready.erase(it);
           }
           if (pack.empty()) break;
           st = arena_launch(s.arena, pack.data(), (int64_t)pack.size(), s.stream);
+          for (size_t k = 0; k < s.ids.size() && st == ACC_OK; ++k) {
+            const acc_serve_req q = placed(s.ids[k]);
+            if (q.host_out) st = acc_download(q.host_out, q.out, out_bytes(q), s.stream);
+          }
           ++batches;
         } else {
-          const int64_t hb = held_bytes(head);
-          if (used + hb > budget_bytes) break;  // wait for memory to free up
+          if (!admit(ready.front())) break;  // wait for memory to free up
           s.ids.push_back(ready.front());
-          s.bytes = hb;
-          used += hb;
           ready.pop_front();
-          st = run_single(head, s.stream);
+          st = launch_one(s.ids.back(), s.stream);
         }
         if (st != ACC_OK) break;
         cudaEventRecord(s.done, s.stream);
@@ -237,22 +337,27 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
     int64_t next = 0;
     while (served < count && st == ACC_OK) {
       bool progress = false;
-      while (!pending.empty() && cudaEventQuery(ring[pending.front() % ring.size()]) == cudaSuccess) {
+      while (!pending.empty()) {
+        const cudaError_t q = cudaEventQuery(ring[pending.front() % ring.size()]);
+        if (q != cudaSuccess && q != cudaErrorNotReady) {
+          st = cuda_status(q);  // the device failed: stop serving
+          break;
+        }
+        if (q != cudaSuccess) break;
         const int64_t id = pending.front();
         pending.pop_front();
         latency[id] = now_s() - reqs[id].arrival;
-        used -= held_bytes(reqs[id]);
+        release(id);
         ++served;
         progress = true;
       }
+      if (st != ACC_OK) break;
       const double t = now_s();
       while (next < count && reqs[next].arrival <= t && (int64_t)pending.size() < (int64_t)ring.size() &&
-             used + held_bytes(reqs[next]) <= budget_bytes) {
-        st = run_single(reqs[next], s);
+             admit(next)) {
+        st = launch_one(next, s);
         if (st != ACC_OK) break;
         cudaEventRecord(ring[next % ring.size()], s);
-        used += held_bytes(reqs[next]);
-        if (used > peak) peak = used;
         pending.push_back(next++);
         if ((int64_t)pending.size() > max_inflight) max_inflight = (int64_t)pending.size();
         progress = true;
@@ -277,6 +382,7 @@ extern "C" int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t b
   }
   for (auto &ev : ring)
     if (ev) cudaEventDestroy(ev);
+  if (arena) cudaFree(arena);
   if (stats) {
     stats->wall_s = wall;
     stats->served = served;

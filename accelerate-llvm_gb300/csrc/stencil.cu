@@ -71,10 +71,7 @@ stencil_kernel(const __grid_constant__ CUtensorMap tin, StencilArgs a, StencilW<
       mbar_expect_tx(&bar, SW * SH * sizeof(T));
       tma_load_2d(tile, &tin, (int)gx0, (int)gy0, &bar);
     }
-    if (!mbar_wait(&bar, 0)) {
-      raise_error(a.err, DEV_ERR_TIMEOUT);
-      mbar_wait(&bar, 0);
-    }
+    if (__syncthreads_or(!mbar_wait_flagged(&bar, 0, a.err))) return;  // the tile never landed
     if (border) {
       // Overwrite the cells the TMA filled with zeros (outside the array).
       for (int k = threadIdx.x; k < SW * SH; k += ST_THREADS) {
@@ -178,10 +175,7 @@ stencil_fast_kernel(const __grid_constant__ CUtensorMap tin, StencilArgs a, Sten
       tma_load_2d(tile, &tin, (int)gx0, (int)gy0, &bar);
     }
     __syncthreads();
-    if (!mbar_wait(&bar, 0)) {
-      raise_error(a.err, DEV_ERR_TIMEOUT);
-      mbar_wait(&bar, 0);
-    }
+    if (__syncthreads_or(!mbar_wait_flagged(&bar, 0, a.err))) return;  // the tile never landed
     if (border) {
       for (int k = threadIdx.x; k < SW * SH; k += ST_THREADS) {
         const int sy = k / SW, sx = k % SW;
@@ -304,9 +298,12 @@ stencil_pipe_kernel(const __grid_constant__ CUtensorMap tin, const __grid_consta
     const int64_t ty = tile / ntx, tx = tile % ntx;
     const int64_t tx0 = tx * SF_TW, ty0 = ty * SF_TH;
     const int64_t gx0 = tx0 - PX, gy0 = ty0 - RY;
-    if (!mbar_wait(&full[s], (uint32_t)(k >> 1) & 1u)) {
-      raise_error(a.err, DEV_ERR_TIMEOUT);
-      mbar_wait(&full[s], (uint32_t)(k >> 1) & 1u);
+    if (__syncthreads_or(!mbar_wait_flagged(&full[s], (uint32_t)(k >> 1) & 1u, a.err))) {
+      // The tile never landed: give the next tile's load, issued into the
+      // other stage, a bounded wait too, then stop (stores already issued
+      // complete below).
+      if (tile + (int64_t)gridDim.x < ntiles) mbar_wait(&full[s ^ 1], (uint32_t)((k + 1) >> 1) & 1u);
+      break;
     }
     T *tile_in = inb(s);
     if (gx0 < 0 || gy0 < 0 || gx0 + SW > a.in_w || gy0 + SH > a.in_h) {

@@ -270,9 +270,7 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "int64+f32+i32",
         "data": "synthetic (seeded, on device): Int64 U[-2^20,2^20], Float32 N(0,1), Int32 Zipf(1.1) bins, Float32 U(0,1)",
-        "config": {"workload": "scanl1 (+) Int64 2^28; fold (+) Float32 2^28; permute (+) histogram 2^28 Int32 "
-                               "Zipf(1.1) -> 2^16 bins; stencil 3x3 Float32 8192^2 clamp",
-                   "l2": "every input > L2 (129 MB); no flush", "parallelism": f"replicas x{world}"},
+        "config": workload_config(world),
         "per_skeleton": per_sk,
         "extra": extra,
         "roofline": {"bound": "hbm", "kernel": "scan_tma_kernel (scanl1 + Int64)", "achieved": round(achieved, 1),
@@ -480,43 +478,9 @@ def run_batched(torch, acc, args, dev, count=10_000):
             "speedup": round(ms_call / ms_batch, 2)}
 
 
-W5 = [[0.0, 0.25, 0.0], [0.25, -1.0, 0.25], [0.0, 0.25, 0.0]]
-
-
-def serving_stream(torch, dev, count, rate, rng, pools):
-    """Mixed requests: 40 % fold, 25 % scanl1, 15 % foldSeg (lognormal
-    segments), 10 % permute histograms into 2^12..2^16 bins, 10 % 5-point
-    Float32 stencils on 256^2..4096^2 grids; sizes log-uniform in
-    [2^10, 2^26]; Poisson arrivals at `rate` per second (rate 0: all at
-    t = 0).  Inputs are slices of device-resident pools; outputs rotate over
-    a pool of output regions."""
-    vals, ivals, off, idx, outs, offs_np = pools
-    kinds = rng.choice(["fold", "scan", "foldseg", "permute", "stencil"], size=count, p=[0.4, 0.25, 0.15, 0.1, 0.1])
-    sizes = np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 26), size=count)).astype(np.int64)
-    t = np.cumsum(rng.exponential(1.0 / rate, size=count)) if rate > 0 else np.zeros(count)
-    reqs = []
-    for i in range(count):
-        k, n = kinds[i], int(sizes[i])
-        out = outs[i % len(outs)]
-        if k in ("fold", "scan"):
-            xs = (vals if i % 2 else ivals)[:n]
-            reqs.append((k, xs, None, out.view(xs.dtype)[: (1 if k == "fold" else n)], n, 0, float(t[i])))
-        elif k == "foldseg":
-            nseg = int(np.searchsorted(offs_np, n, side="right")) - 1
-            nv = int(offs_np[nseg])
-            reqs.append((k, vals[:nv], off, out[:max(nseg, 1)], nv, nseg, float(t[i])))
-        elif k == "permute":
-            m = int(2 ** rng.integers(12, 17))
-            reqs.append((k, idx[m][:n], None, out.view(torch.int32)[:m], n, m, float(t[i])))
-        else:
-            side = int(np.exp(rng.uniform(np.log(256), np.log(4096))))
-            reqs.append((k, vals[:side * side].view(side, side), None, out[:side * side], side, side, float(t[i])))
-    return reqs
-
-
 def request_bytes(r):
     """Algorithmic bytes of one serving request (inputs read + outputs written)."""
-    k, xs, aux, out, n, m, t = r
+    k, xs, aux, out, n, m, t = r[:7]
     e = xs.element_size()
     if k == "fold":
         return n * e + e
@@ -529,10 +493,93 @@ def request_bytes(r):
     return 2 * n * m * e
 
 
+def serving_stream(torch, dev, count, rate, rng, pools, check_every=0):
+    """Mixed requests: 40 % fold, 25 % scanl1, 15 % foldSeg (lognormal
+    segments), 10 % permute histograms into 2^12..2^16 bins, 10 % 5-point
+    Float32 stencils on 256^2..4096^2 grids; sizes log-uniform in
+    [2^10, 2^26]; Poisson arrivals at `rate` per second (rate 0: all at
+    t = 0).  Inputs are slices of device-resident pools; every result is
+    placed by the serving loop in its device arena (output None).  With
+    `check_every` > 0, every check_every-th request whose result has at most
+    2^20 elements also gets a host array that its result is copied back to."""
+    vals, ivals, off, idx, offs_np = pools
+    kinds = rng.choice(["fold", "scan", "foldseg", "permute", "stencil"], size=count, p=[0.4, 0.25, 0.15, 0.1, 0.1])
+    sizes = np.exp(rng.uniform(np.log(2 ** 10), np.log(2 ** 26), size=count)).astype(np.int64)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=count)) if rate > 0 else np.zeros(count)
+    reqs = []
+    for i in range(count):
+        k, n = kinds[i], int(sizes[i])
+        if k in ("fold", "scan"):
+            xs = (vals if i % 2 else ivals)[:n]
+            r = [k, xs, None, None, n, 0, float(t[i])]
+            nres, dt = (1 if k == "fold" else n), xs.dtype
+        elif k == "foldseg":
+            nseg = int(np.searchsorted(offs_np, n, side="right")) - 1
+            nv = int(offs_np[nseg])
+            r = [k, vals[:nv], off, None, nv, nseg, float(t[i])]
+            nres, dt = nseg, torch.float32
+        elif k == "permute":
+            m = int(2 ** rng.integers(12, 17))
+            r = [k, idx[m][:n], None, None, n, m, float(t[i])]
+            nres, dt = m, torch.int32
+        else:
+            side = int(np.exp(rng.uniform(np.log(256), np.log(4096))))
+            r = [k, vals[:side * side].view(side, side), None, None, side, side, float(t[i])]
+            nres, dt = side * side, torch.float32
+        if check_every and i % check_every == 0 and 0 < nres <= (1 << 20):
+            r.append(np.empty(nres, dtype={torch.float32: np.float32, torch.int32: np.int32}[dt]))
+        reqs.append(tuple(r))
+    return reqs
+
+
+def check_served(torch, dev, reqs):
+    """Every result copied back to a host array against a float64 / int64
+    restatement computed with torch on the device: integers exact (wrapping
+    Int32 sums), Float32 sums within 1e-6 |ref| + 1e-9 sum|x|, the stencil
+    within 1e-6 of the grid's magnitude.  Returns the number checked."""
+    checked = 0
+    for r in reqs:
+        if len(r) < 8:
+            continue
+        k, xs, aux, _, n, m, _, host = r
+        got = torch.from_numpy(host).to(dev)
+        if k == "permute":
+            ref = torch.bincount(xs.long(), minlength=m).to(torch.int32)
+            assert torch.equal(got, ref), "served permute differs"
+        elif k == "stencil":
+            g = torch.nn.functional.pad(xs.double()[None, None], (1, 1, 1, 1), mode="replicate")[0, 0]
+            ref = 0.25 * (g[:-2, 1:-1] + g[2:, 1:-1] + g[1:-1, :-2] + g[1:-1, 2:]) - g[1:-1, 1:-1]
+            assert float((got.double().view(n, m) - ref).abs().max()) <= 1e-6 * (1 + float(xs.abs().max())), \
+                "served stencil differs"
+        elif xs.dtype == torch.int32:
+            x64 = xs.long()
+            ref = (x64.sum().view(1) if k == "fold" else torch.cumsum(x64, 0))
+            ref = ((ref + (1 << 31)) % (1 << 32) - (1 << 31)).to(torch.int32)
+            assert torch.equal(got, ref), f"served Int32 {k} differs"
+        else:
+            x64 = xs.double()
+            if k == "fold":
+                ref, absum = x64.sum().view(1), x64.abs().sum().view(1)
+            elif k == "scan":
+                ref, absum = torch.cumsum(x64, 0), torch.cumsum(x64.abs(), 0)
+            else:
+                o = aux[: m + 1].long()
+                seg = torch.repeat_interleave(torch.arange(m, device=dev), o[1:] - o[:-1])
+                xv = x64[: int(o[-1])]
+                ref = torch.zeros(m, dtype=torch.float64, device=dev).index_add_(0, seg, xv)
+                absum = torch.zeros(m, dtype=torch.float64, device=dev).index_add_(0, seg, xv.abs())
+            err = (got.double() - ref).abs()
+            assert bool((err <= 1e-6 * ref.abs() + 1e-9 * absum + 1e-30).all()), f"served {k} differs"
+        checked += 1
+    return checked
+
+
 def run_serving(torch, acc, args, dev):
     """The serving stream at 20k req/s for --serve-seconds, through the
     continuous-batching loop and through plain per-call launches; then each
-    scheduler's capacity with every request arriving at once."""
+    scheduler's capacity with every request arriving at once.  Results are
+    placed by the loop in a device arena of the 40 GB budget (admission
+    waits for room); a sample of them is copied back and checked."""
     rng = np.random.default_rng(SEED + 6)
     g = torch.Generator(device=dev)
     g.manual_seed(SEED + 7)
@@ -541,12 +588,12 @@ def run_serving(torch, acc, args, dev):
     ivals = torch.randint(-1000, 1000, (n_pool,), dtype=torch.int32, device=dev, generator=g)
     off, _, _ = make_segments(torch, dev, n_pool, 1 << 20)
     idx = {m: torch.randint(0, m, (n_pool,), dtype=torch.int32, device=dev, generator=g) for m in [1 << b for b in range(12, 17)]}
-    outs = [torch.empty(n_pool, dtype=torch.float32, device=dev) for _ in range(64)]
-    pools = (vals, ivals, off, idx, outs, off.cpu().numpy().astype(np.int64))
+    pools = (vals, ivals, off, idx, off.cpu().numpy().astype(np.int64))
     budget = 40 << 30
-    res = {"rate_req_s": 20000, "seconds": args.serve_seconds, "budget_bytes": budget, "slots": 8}
+    res = {"rate_req_s": 20000, "seconds": args.serve_seconds, "budget_bytes": budget, "slots": 8,
+           "results": "placed by the loop in a device arena of the budget; admission waits for room"}
     count = int(20000 * args.serve_seconds)
-    stream = serving_stream(torch, dev, count, 20000.0, rng, pools)
+    stream = serving_stream(torch, dev, count, 20000.0, rng, pools, check_every=997)
     for mode in ("batching", "per_call"):
         lat, st = acc.serve(stream, budget, slots=8, mode=mode)
         lat = np.array(lat)
@@ -554,7 +601,9 @@ def run_serving(torch, acc, args, dev):
                      "req_per_s": round(st["served"] / st["wall_s"]),
                      "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
                      "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
-                     "batches": st["batches"], "max_inflight": st["max_inflight"]}
+                     "batches": st["batches"], "max_inflight": st["max_inflight"],
+                     "peak_arena_bytes": st["peak_bytes"],
+                     "checked": check_served(torch, dev, stream)}
     cap_n = min(count, 20000)
     burst = serving_stream(torch, dev, cap_n, 0.0, np.random.default_rng(SEED + 8), pools)
     burst_bytes = sum(request_bytes(r) for r in burst)
@@ -633,17 +682,65 @@ def run_only(args):
     return {"only": name, "scale": args.scale, "ms": round(ms, 4), "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1)}
 
 
+def link_rates(torch, dev, nbytes=1 << 30, trials=5):
+    """This machine's host link with pinned buffers: H2D alone, D2H alone, and
+    both at once (bytes of both directions over the time), each the best of
+    several trials after a warm copy (the link's rate varies a little from
+    moment to moment)."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def best(fn, moved):
+        fn()
+        torch.cuda.synchronize()
+        top = 0.0
+        for _ in range(trials):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s1)
+            s2.wait_event(a)
+            fn()
+            s1.wait_stream(s2)
+            b.record(s1)
+            torch.cuda.synchronize()
+            top = max(top, moved / (a.elapsed_time(b) * 1e-3) / 1e9)
+        return top
+
+    def up():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+
+    def down():
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    def both():
+        up()
+        down()
+
+    r = {"h2d_gbs": best(up, nbytes), "d2h_gbs": best(down, nbytes), "both_gbs": best(both, 2 * nbytes)}
+    del h, h2, d, d2
+    return r
+
+
 def run_e2e(torch, acc, inp, zeros, args, dev):
-    """Same step end to end through the C ABI with host buffers: every step
-    copies each input from pinned host memory, runs the four skeletons
-    (acc_scan, acc_fold, acc_permute_clone, acc_stencil2d on device buffers
-    allocated once) and copies every result back.  Copies in, kernels and
-    copies out run on three streams ordered by events, skeleton by skeleton
-    (scan first, so that its 2 GiB result drains while the other inputs
-    upload)."""
+    """The same step end to end through the library's public API with host
+    buffers (pinned): every step copies each input from host memory into its
+    device copy in a memory table (acc_table_poke), runs the four skeletons
+    on the device copies through the C ABI (acc_scan, acc_fold,
+    acc_permute_clone, acc_stencil2d) and copies every result back to host
+    memory (acc_table_peek).  The table's upload and download streams overlap
+    the copies with each other and with the kernels; the skeletons go in the
+    order scan, fold, permute, stencil, so that the scan's 2 GiB result
+    drains while the other inputs upload.  Device time from the first upload
+    to the last download (CUDA events; the compute stream joins the table's
+    streams at the end)."""
     import ctypes
     lib = acc.lib()
     host = {k: v.cpu().pin_memory() for k, v in inp.items()}
+    host_zeros = zeros.cpu().pin_memory()
     order = [("scan", "scan"), ("fold", "fold"), ("permute", "idx"), ("stencil", "grid")]
     h2d = sum(v.numel() * v.element_size() for v in host.values())
     res_host = {
@@ -653,108 +750,100 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
         "stencil": torch.empty((H_ST, W_ST), dtype=torch.float32).pin_memory(),
     }
     d2h = sum(v.numel() * v.element_size() for v in res_host.values())
-    dev_in = {k: torch.empty_like(v, device=dev) for k, v in host.items()}
-    dev_out = {k: torch.empty_like(v, device=dev) for k, v in res_host.items()}
-    s_in, s_run, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    sp = {k: ctypes.c_void_p(st.cuda_stream) for k, st in (("in", s_in), ("run", s_run), ("out", s_out))}
+    budget = h2d + d2h + host_zeros.numel() * 4 + (64 << 20)
+    tb = acc.Table(budget)
+    stream = torch.cuda.Stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
     zero_f = ctypes.c_float(0.0)
     one_i = ctypes.c_int32(1)
     w9 = (ctypes.c_float * 9)(*[v for r in W9 for v in r])
-    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+    d_zeros = tb.use(host_zeros, stream)  # resident defaults of the histogram, uploaded once
 
-    def run_skeleton(name):
+    def run_skeleton(name, din, dout):
         if name == "scan":
-            st = lib.acc_scan(acc.ADD, acc.I64, 0, 0, 0, ptr(dev_in["scan"]), ptr(dev_out["scan"]), None,
-                              1, N_SCAN, None, sp["run"])
+            st = lib.acc_scan(acc.ADD, acc.I64, 0, 0, 0, vp(din), vp(dout), None, 1, N_SCAN, None, sp)
         elif name == "fold":
-            st = lib.acc_fold(acc.ADD, acc.F32, 0, ptr(dev_in["fold"]), ptr(dev_out["fold"]), 1, N_FOLD,
-                              ctypes.cast(ctypes.pointer(zero_f), ctypes.c_void_p), sp["run"])
+            st = lib.acc_fold(acc.ADD, acc.F32, 0, vp(din), vp(dout), 1, N_FOLD,
+                              ctypes.cast(ctypes.pointer(zero_f), ctypes.c_void_p), sp)
         elif name == "permute":
-            st = lib.acc_permute_clone(acc.ADD, acc.I32, ptr(zeros), None,
-                                       ctypes.cast(ctypes.pointer(one_i), ctypes.c_void_p), ptr(dev_in["idx"]),
-                                       acc.I32, ptr(dev_out["permute"]), N_PERM, M_PERM, sp["run"])
+            st = lib.acc_permute_clone(acc.ADD, acc.I32, vp(d_zeros), None,
+                                       ctypes.cast(ctypes.pointer(one_i), ctypes.c_void_p), vp(din),
+                                       acc.I32, vp(dout), N_PERM, M_PERM, sp)
         else:
             st = lib.acc_stencil2d(acc.F32, 1, 1, ctypes.cast(w9, ctypes.c_void_p), acc.CLAMP, None,
-                                   ptr(dev_in["grid"]), ptr(dev_out["stencil"]), H_ST, W_ST, sp["run"])
+                                   vp(din), vp(dout), H_ST, W_ST, sp)
         if st != 0:
             raise acc.AccError(st, name)
 
-    # Reuse across steps: the next upload into an input buffer waits for the
-    # kernel that read it, and the next kernel into an output buffer waits for
-    # the copy-out that read it.  The waits are enqueued where the buffer is
-    # reused, so that within a step uploads, kernels and copy-outs flow on
-    # their own streams.
-    last_done, last_drained = {}, {}
-
-    def step():
+    def step(first=False, kev=None):
         for name, key in order:
-            ready = torch.cuda.Event()
-            if key in last_done:
-                s_in.wait_event(last_done[key])
-            with torch.cuda.stream(s_in):
-                dev_in[key].copy_(host[key], non_blocking=True)
-                ready.record(s_in)
-            s_run.wait_event(ready)
-            if name in last_drained:
-                s_run.wait_event(last_drained[name])
-            run_skeleton(name)
-            done = torch.cuda.Event()
-            done.record(s_run)
-            s_out.wait_event(done)
-            with torch.cuda.stream(s_out):
-                res_host[name].copy_(dev_out[name], non_blocking=True)
-                drained = torch.cuda.Event()
-                drained.record(s_out)
-            last_done[key] = done
-            last_drained[name] = drained
+            din = tb.use(host[key], stream)  # uploads on the first step only
+            if not first:
+                tb.poke(host[key], stream)   # every step: this step's input
+            dout = tb.malloc(res_host[name], stream)
+            if kev is not None:
+                kev.append((name, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)))
+                kev[-1][1].record(stream)
+            run_skeleton(name, din, dout)
+            if kev is not None:
+                kev[-1][2].record(stream)
+            tb.release(host[key], stream)
+            tb.release(res_host[name], stream)
+            tb.peek(res_host[name], stream)
 
+    step(first=True)
     for _ in range(max(1, args.warmup // 2)):
         step()
+    tb.join(stream)
     torch.cuda.synchronize()
-    # This machine's host link, with the same pinned buffers: the e2e step can be
-    # no faster than its H2D bytes at the H2D rate (the D2H overlaps).  The
-    # host link's rate varies from moment to moment, so the bound takes the
-    # best of several trials after a warm copy.
-    def link_gbs(dst, src, stream, trials=5):
-        best = 0.0
-        with torch.cuda.stream(stream):
-            dst.copy_(src, non_blocking=True)
-            for _ in range(trials):
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                for _ in range(2):
-                    dst.copy_(src, non_blocking=True)
-                b.record(stream)
-                torch.cuda.synchronize()
-                best = max(best, 2 * src.numel() * src.element_size() / (a.elapsed_time(b) * 1e-3) / 1e9)
-        return best
-    h2d_gbs = link_gbs(dev_in["scan"], host["scan"], s_in)
-    d2h_gbs = link_gbs(res_host["scan"], dev_in["scan"], s_out)
+    link = link_rates(torch, dev)
     steps = max(2, args.steps // 2)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(s_in)
-    s_run.wait_event(t0)
-    s_out.wait_event(t0)
+    w0 = time.perf_counter()
+    t0.record(stream)
     for _ in range(steps):
         step()
-    s_out.wait_stream(s_in)
-    s_out.wait_stream(s_run)
-    t1.record(s_out)
+    tb.join(stream)
+    t1.record(stream)
     torch.cuda.synchronize()
-    acc.sync(s_run)
+    wall_ms = (time.perf_counter() - w0) * 1e3 / steps
+    acc.sync(stream)
     ms = t0.elapsed_time(t1) / steps
     # the results that came back are the step's
     assert int(res_host["scan"][-1]) == int(inp["scan"].sum().item())
     assert int(res_host["permute"].sum()) == N_PERM
-    del dev_in, dev_out
-    link_ms = max(h2d / (h2d_gbs * 1e9), d2h / (d2h_gbs * 1e9)) * 1e3
+    # Timeline of two more steps: every transfer of the table (its trace) and
+    # every kernel (events on the compute stream), in ms after one origin.
+    tb.trace(True)
+    origin = torch.cuda.Event(enable_timing=True)
+    origin.record(stream)
+    kev = []
+    for _ in range(2):
+        step(kev=kev)
+    tb.join(stream)
+    torch.cuda.synchronize()
+    timeline = [("kernel " + nm, 0, round(origin.elapsed_time(a), 3), round(origin.elapsed_time(b), 3))
+                for nm, a, b in kev]
+    timeline += [(kind, nb, round(a, 3), round(b, 3)) for kind, nb, a, b in tb.trace_records(origin)]
+    timeline.sort(key=lambda r: r[2])
+    tb.trace(False)
+    stats = tb.stats()
+    tb.close()
+    bound_ms = max(h2d / (link["h2d_gbs"] * 1e9), d2h / (link["d2h_gbs"] * 1e9),
+                   (h2d + d2h) / (link["both_gbs"] * 1e9)) * 1e3
     return {"value": round(sum(BYTES.values()) / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "ms_per_step": round(ms, 3),
+            "wall_ms_per_step": round(wall_ms, 3),
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "link": {"h2d_gbs": round(h2d_gbs, 1), "d2h_gbs": round(d2h_gbs, 1), "bound_ms_per_step": round(link_ms, 2),
-                     "frac_of_link_bound": round(link_ms / ms, 3)},
-            "path": "C ABI entry points (ctypes) on device buffers allocated once; pinned host buffers; "
-                    "H2D / kernels / D2H on three streams"}
+            "link": {k: round(v, 1) for k, v in link.items()} | {
+                "bound_ms_per_step": round(bound_ms, 2), "frac_of_link_bound": round(bound_ms / ms, 3)},
+            "table": {"uploads": stats["uploads"], "downloads": stats["downloads"], "hits": stats["hits"],
+                      "evictions": stats["evictions"]},
+            "timeline_two_steps": timeline,
+            "path": "C ABI: acc_table_use/poke/malloc/peek/release (memory table; pinned host buffers; "
+                    "upload and download streams of the table) + acc_scan/acc_fold/acc_permute_clone/"
+                    "acc_stencil2d on the device copies"}
 
 
 # ----------------------------------------------------------------- CPU arm
@@ -767,7 +856,16 @@ def cpu_inputs(scale):
     p = 1.0 / np.arange(1, M_PERM + 1) ** 1.1
     cdf = np.cumsum(p / p.sum())
     perm = rng.permutation(M_PERM).astype(np.int32)
-    idx = perm[np.minimum(np.searchsorted(cdf, rng.random(n_perm)), M_PERM - 1)]
+    # Inverse CDF through a table of 2^24 equal-probability cells (each cell
+    # holds the bin of its midpoint): the same Zipf(1.1) law to within 2^-24
+    # per bin, at one table lookup per index instead of a binary search.
+    cells = np.minimum(np.searchsorted(cdf, (np.arange(1 << 24) + 0.5) / (1 << 24)), M_PERM - 1)
+    table = perm[cells]
+    idx = np.empty(n_perm, dtype=np.int32)
+    chunk = 1 << 24
+    for s0 in range(0, n_perm, chunk):
+        k = min(chunk, n_perm - s0)
+        idx[s0:s0 + k] = table[rng.integers(0, 1 << 24, size=k, dtype=np.int32)]
     grid = rng.random((h, h), dtype=np.float32)
     return {"scan": x_scan, "fold": x_fold, "idx": idx, "grid": grid, "h": h}
 
@@ -812,6 +910,7 @@ def cpu_model():
 
 def cpu_baseline(scale):
     import oracle
+    scale = scale or 4
     nth = os.cpu_count() or 1
     inp = cpu_inputs(scale)
     cpu_step(oracle, inp, nth)
@@ -825,10 +924,16 @@ def cpu_baseline(scale):
             "per_skeleton_gbs": {k: round(b[k] / sec[k] / 1e9, 2) for k in sec}}
 
 
+def workload_config(world):
+    return {"workload": "scanl1 (+) Int64 2^28; fold (+) Float32 2^28; permute (+) histogram 2^28 Int32 "
+                        "Zipf(1.1) -> 2^16 bins; stencil 3x3 Float32 8192^2 clamp",
+            "l2": "every input > L2 (129 MB); no flush", "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args):
     import oracle
     nth = os.cpu_count() or 1
-    scale = args.cpu_scale
+    scale = args.cpu_scale or 1
     inp = cpu_inputs(scale)
     for _ in range(args.warmup):
         cpu_step(oracle, inp, nth)
@@ -842,11 +947,10 @@ def run_reference(args):
         "value": round(value, 2), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(tot / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64+f32+i32", "data": "synthetic (seeded, host)",
-        "config": {"workload": "scanl1 (+) Int64 2^28; fold (+) Float32 2^28; permute (+) histogram 2^28 Int32 "
-                               "Zipf(1.1) -> 2^16 bins; stencil 3x3 Float32 8192^2 clamp",
-                   "sample": f"1/{scale} of each input per step"},
+        "config": workload_config(args.gpus) if scale == 1 else
+                  dict(workload_config(args.gpus), sample=f"1/{scale} of each input per step"),
         "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": nth, "cpu": cpu_model(), "kind": "port",
-                         "sample": f"1/{scale} of each input per step"},
+                         "sample": "the full inputs" if scale == 1 else f"1/{scale} of each input per step"},
         "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "per_skeleton_gbs": {k: round(b[k] * args.steps / sum(r[k] for r in runs) / 1e9, 2) for k in b},
     }
@@ -900,10 +1004,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-scale", type=int, default=4, help="CPU sample = 1/scale of each input")
+    ap.add_argument("--cpu-scale", type=int, default=None,
+                    help="CPU sample = 1/scale of each input (default: 4 for the CPU baseline beside our arm, "
+                         "1 -- the full inputs -- for --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch workload")
-    ap.add_argument("--serve-seconds", type=float, default=3.0,
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the 20k req/s serving stream (0: skip serving)")
     ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp", "scanzip"],
                     help="time one skeleton alone (small-case driver for ncu captures)")

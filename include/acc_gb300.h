@@ -133,6 +133,23 @@ int acc_sync(void *stream);
  * inside a library call, since those calls hold pointers into the cache. */
 int acc_release_workspaces(void);
 
+/* Make one of the library's bounded device waits run out, on purpose: one
+ * CTA on `stream` waits on something that nothing completes --
+ *   which = 0: an mbarrier phase that no copy and no thread completes (the
+ *              wait every TMA-tiled kernel makes for its tile);
+ *   which = 1: the decoupled look-back of tile 1 of a scan whose tile 0 never
+ *              publishes (the wait of every scan and foldSeg tile on its
+ *              predecessors).
+ * The wait gives up after its limit (2 s of wall-clock time; the mbarrier
+ * wait twice that, since a copy that may still land gets a second wait),
+ * the kernel raises the stream's error word and returns; the next
+ * acc_sync(stream) returns ACC_ERR_TIMEOUT and clears the word, and the
+ * stream is usable as before.
+ * No counterpart in the reference, whose kernels never wait on one another
+ * (its scan runs as separate launches, PTX/Execute.hs:438-468).  For tests
+ * and diagnostics; ACC_ERR_INVALID for another `which`. */
+int acc_selftest_timeout(int which, void *stream);
+
 /* ---------------------------------------------------------------- fold */
 
 /* fold f z / fold1 f along the innermost dimension.
@@ -158,6 +175,18 @@ int acc_fold(int op, int type, int prec, const void *in, void *out,
 int acc_fold_zipwith(int op, int zop, int type, int prec, const void *xs, const void *ys,
                      void *out, int64_t outer, int64_t inner, const void *seed,
                      void *stream);
+
+/* fold f z (map (\x -> g x c) xs) / fold1 f (map ...): a fold whose input is
+ * the fused producer `map` of one array with a primitive g and a constant
+ * operand c (a host pointer to one element of `type`), e.g. the reference's
+ * known answer `A.sum (A.map (+1) xs)` (accelerate-llvm-ptx/test/nofib/Data/
+ * Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs:29).  Replaces foldOp / foldAllOp
+ * on a delayed map input (PTX/CodeGen/Fold.hs:80-97): the mapped array is
+ * never written.  Every mapped element is g x c rounded to `type`; the fold
+ * then follows acc_fold.  op in {ADD, MIN, MAX}, gop in {ADD, MUL, MIN, MAX},
+ * type in {I32, I64, F32, F64}; other combinations give ACC_ERR_UNSUPPORTED. */
+int acc_fold_map(int op, int gop, int type, int prec, const void *xs, const void *c, void *out,
+                 int64_t outer, int64_t inner, const void *seed, void *stream);
 
 /* ---------------------------------------------------------------- foldSeg */
 
@@ -223,6 +252,18 @@ int acc_scan_zipwith(int op, int zop, int type, int prec, int dir, int kind,
                      int64_t outer, int64_t inner, const void *seed,
                      void *stream);
 
+/* Every scan flavour over the fused producer map (\x -> g x c) xs, for a
+ * primitive g and a constant c (a host pointer to one element of `type`):
+ * e.g. scanl1 (+) (map (+1) xs).  Replaces scanOp / scan1Op / scan'Op on a
+ * delayed map input (PTX/CodeGen/Scan.hs:141-439,746-939, the MIRDelayed
+ * argument): the mapped array is never written.  Every mapped element is
+ * g x c rounded to `type`; the scan then follows acc_scan (same `dir`,
+ * `kind`, outputs and errors).  op in {ADD, MIN, MAX}, gop in {ADD, MUL,
+ * MIN, MAX}, type in {I32, I64, F32, F64}; other combinations give
+ * ACC_ERR_UNSUPPORTED. */
+int acc_scan_map(int op, int gop, int type, int prec, int dir, int kind, const void *xs, const void *c,
+                 void *out, void *sums, int64_t outer, int64_t inner, const void *seed, void *stream);
+
 /* acc_scan without any device allocation -- no counterpart in the reference,
  * which always allocates its temporaries (PTX/Execute.hs:453).  Same
  * arguments, results and errors as acc_scan, for callers that cannot let a
@@ -239,11 +280,19 @@ int acc_scan_zipwith(int op, int zop, int type, int prec, int dir, int kind,
  * order, before its kernel runs.  Every call reuses the same array, so calls
  * whose work overlaps on the GPU (other streams, other host threads) race and
  * must be serialised by the caller.  A look-back wait that runs out is not
- * reported by this entry point (acc_sync reports only acc_scan's workspaces);
- * the wait is bounded, so the call always completes. */
+ * reported by acc_sync (which reports only acc_scan's workspaces) but by
+ * acc_scan_noalloc_status; the wait is bounded, so the call always
+ * completes. */
 int acc_scan_noalloc(int op, int type, int prec, int dir, int kind,
                      const void *in, void *out, void *sums, int64_t outer,
                      int64_t inner, const void *seed, void *stream);
+
+/* Wait for the work enqueued on `stream`, then report whether the look-back
+ * wait of the last acc_scan_noalloc call on this device ran out
+ * (ACC_ERR_TIMEOUT; its result is then not to be trusted) or not (ACC_OK).
+ * Allocates nothing: it reads the error word of the same static array.  No
+ * counterpart in the reference. */
+int acc_scan_noalloc_status(void *stream);
 
 /* ---------------------------------------------------------------- permute */
 
@@ -393,10 +442,13 @@ typedef struct acc_serve_req {
   int type;          /* element type (permute: ACC_I32)                      */
   const void *in;
   const void *aux;   /* foldSeg offsets, else unused                          */
-  void *out;
+  void *out;         /* device buffer of the result, or NULL: the loop places
+                        the result in its device arena (see acc_serve_run)    */
   int64_t n;         /* elements (stencil: grid rows)                         */
   int64_t m;         /* foldSeg segments / permute bins / stencil grid columns */
   double arrival;    /* seconds after the start of the run, non-decreasing    */
+  void *host_out;    /* host buffer the result is copied back to before the
+                        request counts as complete, or NULL                  */
 } acc_serve_req;
 
 typedef struct acc_serve_stats {
@@ -409,13 +461,119 @@ typedef struct acc_serve_stats {
 
 /* Serve `reqs` (sorted by arrival) and write each request's latency in
  * seconds (completion seen by the host minus arrival).  mode 0: continuous
- * batching over `slots` streams with a device-memory admission budget of
- * `budget_bytes` (bytes of input + output held by admitted requests);
- * mode 1: plain per-call launches in arrival order on one stream.  The call
- * first synchronises the device (the inputs may still be in flight on the
- * caller's streams) and blocks until every request is served. */
+ * batching over `slots` streams; mode 1: plain per-call launches in arrival
+ * order on one stream.  Admission by device memory, in both modes: the
+ * results of requests with out == NULL are placed in one device arena of
+ * `budget_bytes` (allocated once, before the clock starts), and such a
+ * request is admitted only once its result fits (its range returns when it
+ * completes); requests with their own output buffer are admitted while the
+ * bytes of input and output they hold stay within `budget_bytes`.  A result
+ * with a host_out buffer (pinned or pageable) is copied back before its
+ * request completes.  The call first synchronises the device (the inputs may
+ * still be in flight on the caller's streams) and blocks until every request
+ * is served. */
 int acc_serve_run(const acc_serve_req *reqs, int64_t count, int64_t budget_bytes,
                   int slots, int mode, double *latency, acc_serve_stats *stats);
+
+/* ------------------------------------------------- host <-> device transfer */
+
+/* Copy `bytes` from host memory to device memory (pokeArrayAsync,
+ * PTX/Array/Prim.hs:106-135) or back (peekArrayAsync, :169-195), enqueued on
+ * `stream` and asynchronous to the host.  The host buffer may be pinned
+ * (cudaHostAlloc / cudaHostRegister: copied by the copy engines) or plain
+ * pageable memory (malloc, a GHC pinned byte array, a numpy array): on a GPU
+ * that reads pageable memory through the host's page tables (GB300 with
+ * NVLink-C2C) a copy kernel moves it without staging and without blocking
+ * the calling thread; elsewhere the driver stages it and the call may block
+ * until the copy is done.  The host buffer must stay valid until the copy
+ * has completed (acc_sync on `stream`).  bytes == 0 does nothing. */
+int acc_upload(void *dev, const void *host, int64_t bytes, void *stream);
+int acc_download(void *host, const void *dev, int64_t bytes, void *stream);
+
+/* A memory table: device copies of host arrays kept in one device arena of a
+ * fixed byte budget, allocated once when the table is made, with
+ * least-recently-used eviction.  Replaces the PTX backend's memory table
+ * (PTX/Array/Table.hs:35-49; Remote.malloc / withRemote,
+ * PTX/Array/Remote.hs:60-133) and the transfers the skeleton ops rely on
+ * (useArrayAsync / mallocArray / pokeArrayAsync / peekArrayAsync,
+ * PTX/Array/Prim.hs:72-195; the lazy copy back of copyToHostLazy,
+ * PTX/Array/Data.hs:91-148).  Arrays are keyed by their host address.
+ *
+ * The table owns two streams, one per direction, so that uploads, the
+ * caller's kernels and downloads overlap: an upload runs on the upload
+ * stream and the caller's stream waits for it; a download waits for the
+ * work enqueued so far on the caller's stream and runs on the download
+ * stream.  Between acc_table_use/malloc and acc_table_release an array is
+ * held and never evicted; release records the caller's stream as the last
+ * user, and an evicted array's space is reused only after that work and any
+ * copy back have completed.  An evicted array that the device has written
+ * (since malloc, and not yet copied back by peek) is copied back to its host
+ * array first; one that holds what its host array holds is dropped.  Calls
+ * on one table may come from several host threads (one lock per table). */
+typedef struct acc_table acc_table;
+
+typedef struct acc_table_stats {
+  int64_t budget;          /* bytes of the arena                                */
+  int64_t resident_bytes;  /* bytes held by arrays in the table (rounded)       */
+  int64_t arrays;          /* arrays in the table                               */
+  int64_t uploads, upload_bytes;
+  int64_t downloads, download_bytes;  /* peeks and copies back on eviction      */
+  int64_t hits;            /* acc_table_use calls that found the array resident */
+  int64_t evictions;
+  int64_t writebacks;      /* evictions that copied the array back first        */
+} acc_table_stats;
+
+/* Make a table whose arena holds `budget_bytes` (rounded up to 2 MiB). */
+int acc_table_create(int64_t budget_bytes, acc_table **out);
+/* Wait for the table's work, copy back every array the device has written,
+ * and free the arena and the table's streams. */
+int acc_table_destroy(acc_table *t);
+
+/* useArrayAsync: hold the device copy of the input array [host, host+bytes)
+ * and put its device address in *dev.  If the array is not resident, space
+ * is allocated (evicting as needed) and the array is uploaded; `stream`
+ * waits for the upload.  A resident array is not copied again: its host
+ * array is taken not to change while it is in the table (use poke after a
+ * change).  ACC_ERR_NOMEM when the held arrays leave no room. */
+int acc_table_use(acc_table *t, const void *host, int64_t bytes, void *stream, void **dev);
+/* mallocArray: hold device space for the output array [host, host+bytes),
+ * without any copy; the device copy counts as written from now on. */
+int acc_table_malloc(acc_table *t, void *host, int64_t bytes, void *stream, void **dev);
+/* pokeArrayAsync: copy the host array into its resident device copy again
+ * (after the host array changed); `stream` waits for the copy, which itself
+ * waits for the last recorded user of the device copy. */
+int acc_table_poke(acc_table *t, const void *host, void *stream);
+/* peekArrayAsync: copy the device copy back into its host array once the work
+ * enqueued so far on `stream` is done.  Asynchronous: acc_table_wait (or a
+ * sync of the device) before the host reads the array. */
+int acc_table_peek(acc_table *t, void *host, void *stream);
+/* End the hold taken by use / malloc: the work enqueued so far on `stream`
+ * is the array's last user (withRemote's task). */
+int acc_table_release(acc_table *t, const void *host, void *stream);
+/* Block until every transfer of the array enqueued so far has completed. */
+int acc_table_wait(acc_table *t, const void *host);
+/* Make `stream` wait for every transfer enqueued on the table so far. */
+int acc_table_join(acc_table *t, void *stream);
+/* Drop the array from the table without copying it back (the host array's
+ * finalizer; freeRemote).  ACC_ERR_INVALID while it is held. */
+int acc_table_free(acc_table *t, const void *host);
+int acc_table_get_stats(acc_table *t, acc_table_stats *out);
+
+/* Transfer trace, as the reference times each transfer under its dump_gc
+ * debug flag (PTX/Array/Remote.hs, `transfer`): acc_table_trace(t, 1)
+ * clears the trace and from then on brackets every transfer with timing
+ * events on its stream; acc_table_trace_get waits for the traced transfers
+ * and gives, for the first `cap` of them, the kind (0 upload, 1 download,
+ * 2 copy back on eviction), the bytes and the start / end in milliseconds
+ * after `origin` (a cudaEvent_t created with timing, recorded before the
+ * transfers); *count is the number traced. */
+typedef struct acc_xfer_record {
+  int kind;
+  int64_t bytes;
+  double start_ms, end_ms;
+} acc_xfer_record;
+int acc_table_trace(acc_table *t, int enable);
+int acc_table_trace_get(acc_table *t, void *origin, acc_xfer_record *rec, int64_t cap, int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -94,10 +94,11 @@ int main(void) {
   memset(&sreq, 0, sizeof(sreq));
   expect("serve, no slots", acc_serve_run(&sreq, 1, one << 20, 0, 0, latency, NULL), ACC_ERR_INVALID);
   expect("serve, bad mode", acc_serve_run(&sreq, 1, one << 20, 4, 7, latency, NULL), ACC_ERR_INVALID);
-  sreq.type = ACC_F32; /* a fold with no output buffer */
+  sreq.type = ACC_F32; /* a fold with no input buffer */
   sreq.n = 16;
+  sreq.in = NULL;
+  expect("serve, fold without input", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL), ACC_ERR_INVALID);
   sreq.in = p;
-  expect("serve, fold without output", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL), ACC_ERR_INVALID);
   sreq.type = 9;
   expect("serve, bad element type", acc_serve_run(&sreq, 1, one << 20, 4, 0, latency, NULL), ACC_ERR_INVALID);
   sreq.skeleton = ACC_SK_STENCIL;

@@ -14,14 +14,16 @@ sources (read here as text; nothing of the reference is executed):
     Its expression is spelled `scanr' (+) 10 ...`, but the text and the values
     are those of scanl' (exclusive from the left, total 55 apart), so it is
     recorded as a scanl' known answer.
-Run:  python tests/golden/make_golden.py [path/to/accelerate-llvm checkout]
+Run:  python tests/golden/make_golden.py path/to/accelerate-llvm-checkout
 """
 import json
 import pathlib
 import re
 import sys
 
-ref = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py path/to/accelerate-llvm-checkout")
+ref = pathlib.Path(sys.argv[1])
 runq = (ref / "accelerate-llvm-ptx/test/nofib/Data/Array/Accelerate/LLVM/PTX/NoFib/RunQ.hs").read_text()
 scan = (ref / "accelerate-llvm-native/src/Data/Array/Accelerate/LLVM/Native/CodeGen/Scan.hs").read_text()
 

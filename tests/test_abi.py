@@ -81,6 +81,14 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_fold_seg_zipwith(1, 1, 0, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 2  # fold op (*) unsupported
     assert lib.acc_fold_seg_zipwith(0, 5, 0, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 2  # zipWith (.|.) unsupported
     assert lib.acc_fold_seg_zipwith(0, 1, 2, 0, out, out, out, 0, out, 1, 4, 2, N, N) == 2  # Word32 unsupported
+    # the fused map entry points
+    assert lib.acc_fold_map(0, 0, 0, 0, out, N, out, 1, 4, N, N) == 1      # no constant
+    assert lib.acc_fold_map(0, 9, 0, 0, out, out, out, 1, 4, N, N) == 1    # bad map primitive
+    assert lib.acc_fold_map(0, 0, 0, 0, out, out, out, 2, 0, N, N) == 3    # fold1 of an empty row
+    assert lib.acc_scan_map(0, 0, 0, 0, 7, 0, out, out, out, N, 1, 4, N, N) == 1  # bad direction
+    assert lib.acc_scan_map(0, 0, 0, 0, 0, 1, out, out, out, N, 1, 4, N, N) == 1  # scanl without seed
+    assert lib.acc_scan_map(0, 0, 0, 0, 0, 0, out, N, out, N, 1, 4, N, N) == 1    # no constant
+    assert lib.acc_scan_map(0, 4, 0, 0, 0, 0, out, out, out, N, 1, 4, N, N) == 2  # map (.&. c) unsupported
     # rank-3 stencils
     assert lib.acc_stencil3d(3, 5, 1, 1, out, 0, N, out, out, 4, 4, 4, N) == 1  # radius above 4
     assert lib.acc_stencil3d(3, 1, 1, 1, out, 3, N, out, out, 4, 4, 4, N) == 1  # constant without a value
@@ -97,11 +105,31 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # bad element type
     req = pkg.ServeReq(skeleton=pkg.SK_FOLDSEG, type=3, inp=16, out=16, n=64, m=4)
     assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # foldSeg without offsets
-    req = pkg.ServeReq(skeleton=pkg.SK_SCAN, type=3, inp=16, n=64)
-    assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # scan without output
+    req = pkg.ServeReq(skeleton=pkg.SK_SCAN, type=3, out=16, n=64)
+    assert lib.acc_serve_run(ctypes.byref(req), 1, 1 << 20, 4, 0, lat, N) == 1   # scan without input
     breq = pkg.Request(kind=pkg.REQ_FOLD, type=0, n=0, has_seed=1)                # fold z [] without output
     h = ctypes.c_void_p()
     assert lib.acc_batch_create(0, ctypes.byref(breq), 1, ctypes.byref(h)) == 1
+    # transfers and the memory table
+    assert lib.acc_upload(out, out, -1, N) == 1                                   # negative size
+    assert lib.acc_upload(N, out, 8, N) == 1                                      # no device buffer
+    assert lib.acc_download(out, N, 8, N) == 1                                    # no device buffer
+    assert lib.acc_upload(N, N, 0, N) == 0                                        # nothing to copy
+    assert lib.acc_table_create(0, ctypes.byref(h)) == 1                          # no budget
+    assert lib.acc_table_create(1 << 20, N) == 1                                  # nowhere to put it
+    p = ctypes.c_void_p()
+    assert lib.acc_table_use(N, out, 8, N, ctypes.byref(p)) == 1                  # no table
+    assert lib.acc_table_malloc(N, out, 8, N, ctypes.byref(p)) == 1
+    for f in (lib.acc_table_poke, lib.acc_table_peek, lib.acc_table_release):
+        assert f(N, out, N) == 1
+    assert lib.acc_table_wait(N, out) == 1
+    assert lib.acc_table_free(N, out) == 1
+    assert lib.acc_table_destroy(N) == 1
+    assert lib.acc_table_join(N, N) == 1
+    assert lib.acc_table_get_stats(N, N) == 1
+    assert lib.acc_table_trace(N, 1) == 1
+    assert lib.acc_table_trace_get(N, out, N, 0, N) == 1
+    assert lib.acc_selftest_timeout(7, N) == 1                                    # no such wait
 
 
 def test_c_caller_links_and_validates(lib, tmp_path):

@@ -107,3 +107,29 @@ def test_request_larger_than_budget_is_rejected(acc, dev):
     with pytest.raises(acc.AccError) as e:
         acc.serve([("fold", xs, None, out, xs.numel(), 0, 0.0)], budget_bytes=1024)
     assert e.value.status == 8
+
+
+NP = {torch.int32: np.int32, torch.int64: np.int64, torch.float32: np.float32, torch.float64: np.float64}
+
+
+@pytest.mark.parametrize("mode", ["batching", "per_call"])
+def test_results_in_the_arena_copied_back(acc, dev, mode):
+    """Results placed by the loop in its device arena (no output buffer),
+    each copied back to a host array, under a budget small enough that
+    admission waits for arena room; every copied-back result equals the
+    request run alone."""
+    reqs = make_stream(dev, count=160, rate=1e6, seed=5)
+    placed = []
+    for k, xs, aux, out, n, m, t in reqs:
+        placed.append((k, xs, aux, None, n, m, t, np.full(out.numel(), 7, dtype=NP[out.dtype])))
+    budget = 4 << 20
+    lat, stats = acc.serve(placed, budget_bytes=budget, slots=8, mode=mode)
+    assert stats["served"] == len(placed)
+    assert 0 < stats["peak_bytes"] <= budget
+    bad = []
+    for i, (r, p) in enumerate(zip(reqs, placed)):
+        ref = alone(acc, r)
+        got = torch.from_numpy(p[7]).to(dev).view(r[3].shape)
+        if not same(r[0], got, ref, r[1]):
+            bad.append(i)
+    assert not bad, f"{len(bad)} requests differ, first {reqs[bad[0]][0]} #{bad[0]}"

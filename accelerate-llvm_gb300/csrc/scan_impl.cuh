@@ -465,6 +465,7 @@ constexpr int L2S_COMPUTE = SCAN_THREADS;
 constexpr int L2S_THREADS = L2S_COMPUTE + 32;
 constexpr int L2S_TILE = SCAN_THREADS * SCAN_ROW_BYTES;
 constexpr int L2S_CTAS_PER_SM = 3;
+constexpr bool L2S_HINTS = true;  // L2 policies: keep a tile between its two loads, drop it after
 
 template <int OP, class T, int PREC, bool R2L>
 __global__ void __launch_bounds__(L2S_THREADS, L2S_CTAS_PER_SM)
@@ -499,7 +500,8 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     s_claim = d;
     if (d < a.ntiles) {
       mbar_expect_tx(&fullA, L2S_TILE);
-      tma_load_2d(bufA, &tin, 0, (int)(tile_of(d) * SCAN_THREADS), &fullA);
+      if constexpr (L2S_HINTS) tma_load_2d_hint(bufA, &tin, 0, (int)(tile_of(d) * SCAN_THREADS), &fullA, l2_policy_evict_last());
+      else tma_load_2d(bufA, &tin, 0, (int)(tile_of(d) * SCAN_THREADS), &fullA);
     }
   }
   __syncthreads();
@@ -559,6 +561,14 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     const int pn = (int)(k & 1), pc = pn ^ 1;
     int64_t t_new = -1;
     S excl_new = A::id();
+    if (t_cur >= 0 && tid == 0) {
+      // the current tile's second load (from L2) runs during the next tile's fold
+      tma_store_wait_read();  // the previous store has read B
+      mbar_expect_tx(&fullB, L2S_TILE);
+      if constexpr (L2S_HINTS) tma_load_2d_hint(bufB, &tin, 0, (int)(t_cur * SCAN_THREADS), &fullB, l2_policy_evict_first());
+      else tma_load_2d(bufB, &tin, 0, (int)(t_cur * SCAN_THREADS), &fullB);
+    }
+    if (t_cur >= 0) b_loading = true;
     if (have_new) {
       // pass 1 of the new tile (in A)
       t_new = tile_of(d_new);
@@ -598,7 +608,8 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         s_claim = dn;
         if (dn < a.ntiles) {
           mbar_expect_tx(&fullA, L2S_TILE);
-          tma_load_2d(bufA, &tin, 0, (int)(tile_of(dn) * SCAN_THREADS), &fullA);
+          if constexpr (L2S_HINTS) tma_load_2d_hint(bufA, &tin, 0, (int)(tile_of(dn) * SCAN_THREADS), &fullA, l2_policy_evict_last());
+          else tma_load_2d(bufA, &tin, 0, (int)(tile_of(dn) * SCAN_THREADS), &fullA);
         }
       }
     } else if (tid == 0) {
@@ -606,14 +617,8 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       mbar_arrive(&aggr[pn]);
     }
     if (t_cur >= 0) {
-      // pass 2 of the current tile: load it again (from L2) into B, rescan it
+      // pass 2 of the current tile (loaded again, from L2, into B): rescan it
       // from its prefix, store it
-      if (tid == 0) {
-        tma_store_wait_read();  // the previous store has read B
-        mbar_expect_tx(&fullB, L2S_TILE);
-        tma_load_2d(bufB, &tin, 0, (int)(t_cur * SCAN_THREADS), &fullB);
-      }
-      b_loading = true;
       const bool okp = mbar_wait_flagged(&pref[pc], (uint32_t)((k - 1) >> 1) & 1u, a.err);
       const bool okb = mbar_wait_flagged(&fullB, phB, a.err);
       if (named_bar_or<1, L2S_COMPUTE>(!(okp && okb))) { failed = true; break; }
@@ -656,7 +661,8 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       fence_proxy_async_smem();
       named_bar_sync<1, L2S_COMPUTE>();
       if (tid == 0) {
-        tma_store_2d(&tout, 0, (int)(t_cur * SCAN_THREADS), bufB);
+        if constexpr (L2S_HINTS) tma_store_2d_hint(&tout, 0, (int)(t_cur * SCAN_THREADS), bufB, l2_policy_evict_first());
+        else tma_store_2d(&tout, 0, (int)(t_cur * SCAN_THREADS), bufB);
         tma_store_commit();
       }
     }

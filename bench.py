@@ -273,7 +273,7 @@ def run_ours(args, rank, world):
         "config": workload_config(world),
         "per_skeleton": per_sk,
         "extra": extra,
-        "roofline": {"bound": "hbm", "kernel": "scan_tma_kernel (scanl1 + Int64)", "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": "scan_l2_kernel (scanl1 + Int64)", "achieved": round(achieved, 1),
                      "peak": peak, "peak_kind": f"{peak_kind} hbm_gbs (copy)", "unit": "GB/s",
                      "frac": round(achieved / peak, 3),
                      "traffic": NCU_TRAFFIC["scan"]},

@@ -51,7 +51,7 @@ BYTES = {
 # processed to the full launch (traffic grows in proportion; the stencil case
 # is already full size).  Summaries with the commands sit in profiles/.
 NCU_TRAFFIC = {
-    "scan": int((268.570368e6 + 213.748992e6) * 8),   # 2^25 Int64 -> 2^28
+    "scan": int((270.588416e6 + 207.724288e6) * 8),   # 2^25 Int64 -> 2^28 (scan_l2_kernel)
     "fold": int((268.478208e6 + 2.757376e6) * 4),     # 2^26 Float32 -> 2^28
     "permute": int((268.722688e6 + 2.906368e6) * 4),  # 2^26 indices -> 2^28
     "stencil": int(292.122624e6 + 222.595328e6),      # 8192^2, full size

@@ -201,6 +201,24 @@ cudaEvent_t make_event() {
   return ev;
 }
 
+// Record `ev` anew on stream q as a fresh event object (the old one is
+// released once its waiters are done).  Re-recording one event object that
+// other streams wait on serialised the table's upload and download streams
+// on GB300: a step of the bench's end-to-end leg took 30 to 60 ms instead of
+// 25 ms, the host link's bound being 22 ms.
+int record_fresh(cudaEvent_t &ev, cudaStream_t q) {
+  cudaEvent_t fresh = make_event();
+  if (!fresh) return ACC_ERR_CUDA;
+  const cudaError_t ce = cudaEventRecord(fresh, q);
+  if (ce != cudaSuccess) {
+    cudaEventDestroy(fresh);
+    return cuda_status(ce);
+  }
+  if (ev) cudaEventDestroy(ev);
+  ev = fresh;
+  return ACC_OK;
+}
+
 // Evict entry e (not held): its range is reused once its last user and any
 // copy back are done.  writeback: copy a device-written array back first.
 int retire(acc_table *t, acc_table::Entry &e, bool writeback) {
@@ -313,8 +331,8 @@ int upload(acc_table *t, acc_table::Entry &e, cudaEvent_t after) {
   if (e.has_xfer) cudaStreamWaitEvent(t->up, e.xfer, 0);
   int st = traced_copy(t, 0, t->arena + e.off, e.host, e.host, e.bytes, t->up);
   if (st) return st;
-  cudaError_t ce = cudaEventRecord(e.xfer, t->up);
-  if (ce != cudaSuccess) return cuda_status(ce);
+  const int rs = record_fresh(e.xfer, t->up);
+  if (rs) return rs;
   e.has_xfer = true;
   e.dirty = false;
   t->st.uploads += 1;
@@ -479,8 +497,8 @@ extern "C" int acc_table_peek(acc_table *t, void *host, void *stream) {
   if (e.has_xfer) cudaStreamWaitEvent(t->down, e.xfer, 0);
   st = traced_copy(t, 1, host, t->arena + e.off, host, e.bytes, t->down);
   if (st) return st;
-  cudaError_t ce = cudaEventRecord(e.xfer, t->down);
-  if (ce != cudaSuccess) return cuda_status(ce);
+  st = record_fresh(e.xfer, t->down);
+  if (st) return st;
   e.has_xfer = true;
   e.dirty = false;
   e.tick = ++t->tick;
@@ -499,8 +517,8 @@ extern "C" int acc_table_release(acc_table *t, const void *host, void *stream) {
   // Several holders on different streams: the recorded last user follows
   // every one of them.
   if (e.has_use) cudaStreamWaitEvent(s, e.last_use, 0);
-  cudaError_t ce = cudaEventRecord(e.last_use, s);
-  if (ce != cudaSuccess) return cuda_status(ce);
+  const int rs = record_fresh(e.last_use, s);
+  if (rs) return rs;
   e.has_use = true;
   e.holds -= 1;
   return ACC_OK;

@@ -347,10 +347,13 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
   __shared__ int64_t s_tile, s_kf, s_cnt, s_lo, s_hi, s_first_id;
   __shared__ int s_offs[FT_CAP];
   __shared__ int s_rowh[FT_THREADS];  // per thread: first offset entry at or after its first value
-  __shared__ S s_res[FT_CAP];         // per entry: the state of the segment that ends there
+  __shared__ S s_res[FT_CAP];         // per entry (or, in a slot tile, per boundary): a closed segment's state
   __shared__ S s_wv[NWARP], s_first_v, s_tile_v;
   __shared__ int s_wf[NWARP];
   __shared__ int s_has_first, s_tile_f, s_bad;
+  __shared__ uint64_t s_bm[FT_THREADS];  // slot tiles: each thread's boundary positions
+  __shared__ int s_base[FT_THREADS];     // slot tiles: each thread's first boundary slot
+  __shared__ int s_nbw[NWARP];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const OT *off = static_cast<const OT *>(a.off);
   T *out = static_cast<T *>(a.out);
@@ -453,6 +456,62 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
   S acc = A::id(), left = A::id();
   bool started = false;
   int64_t first_h = -1;
+  // A slot tile (the common case: well-formed offsets, all in shared memory,
+  // every value of the tile inside the segments, no partial row) parks the
+  // closed states by BOUNDARY: thread t's boundaries take slots s_base[t],
+  // s_base[t]+1, ... (an exclusive scan of the threads' boundary counts), so
+  // the walk keeps one running slot index and has no branch per value;
+  // several offsets at one position (empty segments) are one boundary.  The
+  // result pass finds a segment's slot from its position.
+  const bool slot_tile = ok && cnt <= FT_CAP && lo == 0 && hi == TE &&
+                         (tile + 1) * (int64_t)(FT_RPT * FT_THREADS) <= a.full_rows;
+  int pbase = 0;
+  if (slot_tile) {
+    int64_t he = tid + 1 < FT_THREADS ? (int64_t)s_rowh[tid + 1] : cnt;
+    if (he < h || he > cnt) he = cnt;
+    uint64_t bm = 0;
+    for (int64_t e = h; e < he; ++e) {
+      const int r = s_offs[e] - tb0;
+      if (r >= 0 && r < W) bm |= 1ull << r;
+    }
+    const int nb = __popcll(bm);
+    int incl = nb;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int o = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += o;
+    }
+    if (lane == 31) s_nbw[warp] = incl;
+    __syncthreads();
+    int wbase = 0;
+    for (int w2 = 0; w2 < warp; ++w2) wbase += s_nbw[w2];
+    pbase = wbase + incl - nb;
+    s_bm[tid] = bm;
+    s_base[tid] = pbase;
+    int pk = pbase;
+#pragma unroll 1
+    for (int c = 0; c < W / VEC; ++c) {
+      const int r = FT_RPT * tid + c / (ITEMS / VEC);
+      const int cc = c % (ITEMS / VEC);
+      const int rr = r % FT_THREADS;
+      const uint4 v = *reinterpret_cast<const uint4 *>(buf + (r / FT_THREADS) * SUB_BYTES + rr * FT_ROW_BYTES +
+                                                       ((cc ^ (rr & 7)) << 4));
+      T x[VEC];
+      memcpy(x, &v, 16);
+      const uint32_t cb = (uint32_t)(bm >> (c * VEC)) & ((1u << VEC) - 1u);
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) {
+        const bool bnd = (cb >> q) & 1u;
+        if (bnd) s_res[pk] = acc;
+        pk += bnd ? 1 : 0;
+        acc = bnd ? A::id() : acc;
+        acc = A::push(acc, x[q]);
+      }
+    }
+    started = nb > 0;
+    first_h = h;  // the entry of the thread's first boundary
+    if (started) left = s_res[pbase];
+  } else {
   // A boundary only parks the closed segment's state (the results leave in
   // one coalesced pass after the scan), so a lane that meets one holds its
   // warp up for a few instructions.
@@ -558,6 +617,8 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
     }
   }
 
+  }
+
   // ---- segmented CTA scan of the rows' carried-out values
   S iv = acc;
   bool ifl = started;
@@ -586,7 +647,8 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
   if (started) {
     const S v = A::comb(cin, left);
     if (cinf) {
-      if (first_h < FT_CAP) s_res[first_h] = v;
+      if (slot_tile) s_res[pbase] = v;
+      else if (first_h < FT_CAP) s_res[first_h] = v;
       else if (ok) out[kf + first_h - 1] = A::lower(a.has_seed ? A::comb(A::lift(z), v) : v);
     } else {
       s_first_v = v;  // the tile's first boundary: needs the value from earlier tiles
@@ -607,7 +669,13 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
     const int64_t nres = cnt < FT_CAP ? cnt : FT_CAP;
     for (int64_t e = 1 + tid; e < nres; e += FT_THREADS)
       if (s_offs[e] > s_offs[e - 1]) {  // the first entry at its position closes a segment
-        const S v = s_res[e];
+        int slot = (int)e;
+        if (slot_tile) {
+          // the boundary at position p is bit p % W of thread p / W
+          const int p = s_offs[e], t = p / W, bit = p % W;
+          slot = s_base[t] + __popcll(s_bm[t] & ((1ull << bit) - 1ull));
+        }
+        const S v = s_res[slot];
         out[kf + e - 1] = A::lower(a.has_seed ? A::comb(A::lift(z), v) : v);
       }
   }

@@ -646,6 +646,15 @@ def run_only(args):
         xs = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
         ys = torch.randn(N_FOLD // args.scale, dtype=torch.float32, device=dev, generator=g)
         fn, nbytes = (lambda: acc.dotp(xs, ys)), 8 * xs.numel()
+    elif name == "stencil3d":
+        # 3x3x3 Float32 stencil (weights 1/27) on a 512^3 grid / scale, clamp:
+        # 8 B/element (read + write)
+        g = torch.Generator(device=dev)
+        g.manual_seed(SEED + 11)
+        side = max(8, int(round(512 / args.scale ** (1.0 / 3.0))))
+        grid3 = torch.rand((side, side, side), dtype=torch.float32, device=dev, generator=g)
+        w27 = [[[1.0 / 27] * 3] * 3] * 3
+        fn, nbytes = (lambda: acc.stencil3d(w27, grid3, "clamp")), 8 * grid3.numel()
     elif name == "scanzip":
         # scanl1 (+) (zipWith (*) xs ys) on Float32 with the zipWith fused into
         # the scan: 12 B/element (two reads, one write)
@@ -797,7 +806,6 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
         step()
     tb.join(stream)
     torch.cuda.synchronize()
-    link = link_rates(torch, dev)
     steps = max(2, args.steps // 2)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -831,6 +839,10 @@ def run_e2e(torch, acc, inp, zeros, args, dev):
     tb.trace(False)
     stats = tb.stats()
     tb.close()
+    # The host link's rates, measured after the timed steps: on a GB300 a
+    # probe of fresh pinned buffers run before them left every later step at
+    # about half the link's rate (58 ms instead of 24.5 ms per step).
+    link = link_rates(torch, dev)
     bound_ms = max(h2d / (link["h2d_gbs"] * 1e9), d2h / (link["d2h_gbs"] * 1e9),
                    (h2d + d2h) / (link["both_gbs"] * 1e9)) * 1e3
     return {"value": round(sum(BYTES.values()) / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "ms_per_step": round(ms, 3),
@@ -1011,7 +1023,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-launch workload")
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the 20k req/s serving stream (0: skip serving)")
-    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp", "scanzip"],
+    ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp", "scanzip",
+                                       "stencil3d"],
                     help="time one skeleton alone (small-case driver for ncu captures)")
     ap.add_argument("--scale", type=int, default=1, help="with --only: 1/scale of the full input")
     args = ap.parse_args()

@@ -202,7 +202,7 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
           if (exists && flag == 0) flag = b_peek<S>(a.status, pt, epoch, v);
           if (__all_sync(0xffffffffu, flag != 0)) break;
           ++it;
-          if (it == 1) t_wait = global_ns();
+          if (it == 8) t_wait = global_ns();  // first checked at it == 64
           const bool stop = gave_up || it > SPIN_LIMIT ||
                             ((it & 63u) == 0 && ((ld_relaxed_u32(a.words) & DEV_ERR_TIMEOUT) != 0u ||
                                                  global_ns() - t_wait > WAIT_LIMIT_NS));

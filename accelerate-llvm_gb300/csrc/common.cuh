@@ -399,7 +399,9 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t phase) {
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done) : "r"(addr), "r"(phase) : "memory");
     if (done) return true;
-    if (it == 0) t0 = global_ns();
+    // The clock starts only once the wait is a long one: a wait that ends
+    // within 64 polls (the usual TMA landing) reads no timer.
+    if (it == 64) t0 = global_ns();
     if (it > 64) {
       if ((it & 15u) == 0 && global_ns() - t0 > WAIT_LIMIT_NS) return false;
       __nanosleep(64);

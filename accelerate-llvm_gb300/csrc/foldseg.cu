@@ -711,7 +711,7 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
           kp = lb_window<LB>(fl, resolved, whole);
           if (resolved || whole) break;
           ++it;
-          if (it == 1) t_wait = global_ns();
+          if (it == 8) t_wait = global_ns();  // first checked at it == 64
           const bool stop = gave_up || it > SPIN_LIMIT ||
                             ((it & 63u) == 0 && ((ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u ||
                                                  global_ns() - t_wait > WAIT_LIMIT_NS));

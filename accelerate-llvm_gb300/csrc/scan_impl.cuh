@@ -151,7 +151,7 @@ __device__ __forceinline__ typename A::S lookback_prefix(const ScanArgs &a, int6
       ++it;
       // Give up (warp-uniformly) after WAIT_LIMIT_NS or SPIN_LIMIT polls, or
       // at once when another CTA on this stream has already timed out.
-      if (it == 1) t_wait = global_ns();
+      if (it == 8) t_wait = global_ns();  // first checked at it == 64
       const bool stop = gave_up || it > SPIN_LIMIT ||
                         ((it & 63u) == 0 && ((ld_relaxed_u32(a.err) & DEV_ERR_TIMEOUT) != 0u ||
                                              global_ns() - t_wait > WAIT_LIMIT_NS));

@@ -266,6 +266,7 @@ stencil_pipe_kernel(const __grid_constant__ CUtensorMap tin, const __grid_consta
   auto inb = [&](int s) { return reinterpret_cast<T *>(base + s * IN_BYTES); };
   auto outb = [&](int s) { return reinterpret_cast<T *>(base + 2 * IN_BYTES + s * OUT_BYTES); };
   __shared__ uint64_t full[2];
+  __shared__ int s_abort;
   const int tid = threadIdx.x;
   const T *in = static_cast<const T *>(a.in);
 
@@ -277,6 +278,7 @@ stencil_pipe_kernel(const __grid_constant__ CUtensorMap tin, const __grid_consta
   if (tid == 0) {
     prefetch_tmap(&tin);
     prefetch_tmap(&tout);
+    s_abort = 0;
     mbar_init(&full[0], 1);
     mbar_init(&full[1], 1);
     fence_mbar_init();
@@ -298,13 +300,10 @@ stencil_pipe_kernel(const __grid_constant__ CUtensorMap tin, const __grid_consta
     const int64_t ty = tile / ntx, tx = tile % ntx;
     const int64_t tx0 = tx * SF_TW, ty0 = ty * SF_TH;
     const int64_t gx0 = tx0 - PX, gy0 = ty0 - RY;
-    if (__syncthreads_or(!mbar_wait_flagged(&full[s], (uint32_t)(k >> 1) & 1u, a.err))) {
-      // The tile never landed: give the next tile's load, issued into the
-      // other stage, a bounded wait too, then stop (stores already issued
-      // complete below).
-      if (tile + (int64_t)gridDim.x < ntiles) mbar_wait(&full[s ^ 1], (uint32_t)((k + 1) >> 1) & 1u);
-      break;
-    }
+    // A tile that never lands sets s_abort; the CTA stops at the next
+    // barrier, before it stores from or loads into its buffers (no extra
+    // barrier per tile).
+    if (!mbar_wait_flagged(&full[s], (uint32_t)(k >> 1) & 1u, a.err)) s_abort = 1;
     T *tile_in = inb(s);
     if (gx0 < 0 || gy0 < 0 || gx0 + SW > a.in_w || gy0 + SH > a.in_h) {
       for (int q = tid; q < SW * SH; q += ST_THREADS) {
@@ -347,6 +346,15 @@ stencil_pipe_kernel(const __grid_constant__ CUtensorMap tin, const __grid_consta
     // The store issued from this output buffer two tiles ago must have read it.
     if (tid == 0 && k >= 2) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
     __syncthreads();
+    if (s_abort) {
+      // bounded waits for this tile's load and the next one, issued into the
+      // other stage, then stop (stores already issued complete below)
+      if (tid == 0) {
+        mbar_wait(&full[s], (uint32_t)(k >> 1) & 1u);
+        if (tile + (int64_t)gridDim.x < ntiles) mbar_wait(&full[s ^ 1], (uint32_t)((k + 1) >> 1) & 1u);
+      }
+      break;
+    }
     T *ob = outb(s);
 #pragma unroll
     for (int r = 0; r < SF_ROWS; ++r) ob[(oy0 + r) * SF_TW + col] = acc[r];

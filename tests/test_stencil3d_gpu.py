@@ -61,6 +61,40 @@ def test_stencil3d_box_clamp(acc, orc, dev):
     check(acc, orc, dev, np.float32, w, g, 0, np.float32(0))
 
 
+def dense_or_star(dt, kind, rng):
+    w = weights(dt, (3, 3, 3), rng)
+    if kind == "dense":
+        w[w == 0] = 1
+    else:  # the 7-point star: the centre and its six face neighbours
+        star = np.zeros((3, 3, 3), dtype=bool)
+        star[1, 1, :] = star[1, :, 1] = star[:, 1, 1] = True
+        w[~star] = 0
+        w[star & (w == 0)] = 2
+    return w
+
+
+@pytest.mark.parametrize("t", list(STYPES))
+@pytest.mark.parametrize("b", [0, 1, 2, 3])
+@pytest.mark.parametrize("kind", ["dense", "star"])
+def test_stencil3d_streaming_patterns(acc, orc, dev, t, b, kind):
+    """The 3x3x3 plane-streaming kernel's compile-time tap patterns, over
+    rows that are 16-byte aligned (copied in 16-byte pieces) and rows that
+    are not, from an array that starts one element past a 16-byte boundary,
+    and plane counts that split into several plane ranges."""
+    dt = STYPES[t]
+    rng = case_rng("stencil3d_stream", t, b, kind)
+    for shape in [(1, 1, 1), (5, 6, 7), (9, 40, 64), (33, 35, 96), (3, 70, 200), (300, 4, 8)]:
+        w = dense_or_star(dt, kind, rng)
+        x = data(dt, shape, rng)
+        check(acc, orc, dev, dt, w, x, b, dt(7))
+        # the same array one element into its allocation
+        flat = torch.zeros(x.size + 1, dtype=torch.from_numpy(x).dtype, device=dev)
+        flat[1:] = torch.from_numpy(x.ravel()).to(dev)
+        got = acc.stencil3d(w.tolist(), flat[1:].view(shape), b, cval=dt(7)).cpu().numpy()
+        ref = orc.stencil3d(w, x, b, cval=dt(7))
+        assert np.array_equal(got, ref), f"offset {shape}: {_diff(got, ref)}"
+
+
 def test_stencil3d_errors(acc, dev):
     x = torch.zeros((4, 4, 4), dtype=torch.float32, device=dev)
     with pytest.raises(ValueError):

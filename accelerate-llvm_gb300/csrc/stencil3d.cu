@@ -229,6 +229,9 @@ stencil3d_stream_kernel(const __grid_constant__ Stencil3Args a, const __grid_con
   }
   const int64_t gx = x0 + tx;
   const int64_t gyt = y0 + ty * S3S_ROWS;
+  T wr[K * K * K];  // the weights, in registers (read once from the parameter)
+#pragma unroll
+  for (int t = 0; t < K * K * K; ++t) wr[t] = W.w[t];
   int buf = 0;
   auto step = [&](int64_t p, auto rot) {
     constexpr int ROT = decltype(rot)::value;
@@ -258,7 +261,7 @@ stencil3d_stream_kernel(const __grid_constant__ Stencil3Args a, const __grid_con
             const int t = ((2 * R - k) * K + dyi) * K + dx;
             if (!s3_tap<PAT>(t, mask)) continue;
             T &ac = acc[(k + ROT) % K][r];
-            ac = fma_tap(W.w[t], xv[dx], ac);
+            ac = fma_tap(wr[t], xv[dx], ac);
           }
         }
       }

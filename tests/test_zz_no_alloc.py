@@ -158,3 +158,29 @@ def test_noalloc_rejects_rows_beyond_its_scratch(acc, dev):
     x = torch.zeros(16, dtype=torch.int64, device=dev)
     # 2^28 + 1 elements per row exceed the 2 MiB scratch: rejected before any launch
     assert _call(acc, lib.acc_scan_noalloc, 0, I64, 0, 0, x, x, None, 1, (1 << 28) + 1, None) == 8
+
+
+def test_noalloc_graph_replays_see_new_input(acc, orc, dev):
+    """The use the entry point is for: one call captured into a CUDA graph
+    (after a first call outside capture), then replayed with new input in
+    the same buffer.  Every replay clears its status slots in stream order,
+    so no tile takes a prefix left by an earlier replay."""
+    lib = acc.lib()
+    n = (1 << 22) + 3
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(17)
+    x = torch.randint(-1000, 1000, (n,), dtype=torch.int64, device=dev, generator=gen)
+    out = torch.empty_like(x)
+    assert _call(acc, lib.acc_scan_noalloc, 0, I64, 0, 0, x, out, None, 1, n, None) == 0
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        st = _call(acc, lib.acc_scan_noalloc, 0, I64, 0, 0, x, out, None, 1, n, None)
+    assert st == 0
+    for step in range(3):
+        x.copy_(torch.randint(-1000, 1000, (n,), dtype=torch.int64, device=dev, generator=gen))
+        out.fill_(0)
+        g.replay()
+        torch.cuda.synchronize()
+        assert lib.acc_scan_noalloc_status(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+        assert np.array_equal(out.cpu().numpy(), orc.scan("+", None, x.cpu().numpy(), 0, 0)), f"replay {step}"

@@ -440,6 +440,25 @@ scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__
   if (tid == 0) tma_store_wait_read();
 }
 
+// Zip one thread's 128-byte row of the two swizzled tiles into the first:
+// buf[row] = g buf[row] buf2[row], element by element.
+template <class T, int Z>
+__device__ __forceinline__ void zip_row(unsigned char *buf, const unsigned char *buf2, int row) {
+  constexpr int VEC = 16 / sizeof(T);
+#pragma unroll
+  for (int c = 0; c < SCAN_ROW_BYTES / 16; ++c) {
+    uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(row, c));
+    const uint4 w = *reinterpret_cast<const uint4 *>(buf2 + swz(row, c));
+    T x[VEC], y[VEC];
+    memcpy(x, &v, 16);
+    memcpy(y, &w, 16);
+#pragma unroll
+    for (int k = 0; k < VEC; ++k) x[k] = Prim<Z, T>::ap(x[k], y[k]);
+    memcpy(&v, x, 16);
+    *reinterpret_cast<uint4 *>(buf + swz(row, c)) = v;
+  }
+}
+
 // --------------------------------------------------------------------------
 // Persistent single-pass scan with a re-read from L2, for 16-byte aligned
 // 1-D arrays.  A tile (32 KiB: 256 rows x 128 B, thread t owns row t) is
@@ -461,15 +480,23 @@ scan_tma_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__
 // tile's prefix, so the lowest unfinished tile can always finish.  Every
 // wait is bounded: a wait that runs out stops the CTA (after a bounded wait
 // for its copies in flight) and raises DEV_ERR_TIMEOUT.
+// PROD selects the scanned array's producer (the reference's delayed scan
+// input, PTX/CodeGen/Scan.hs:141-439): 0 = the array itself; 1 = map
+// (\x -> g x c), applied as each row is read, in both passes; 2 = zipWith g
+// xs ys: pass 1 loads the tiles of both arrays (into A and Y), zips them in
+// place in A and, besides folding, stores the zipped tile to its place in the
+// output, where pass 2 finds it in L2; the zipped array thus costs no DRAM
+// traffic and the CTA needs 96 KiB (two per SM).
 constexpr int L2S_COMPUTE = SCAN_THREADS;
 constexpr int L2S_THREADS = L2S_COMPUTE + 32;
 constexpr int L2S_TILE = SCAN_THREADS * SCAN_ROW_BYTES;
 constexpr int L2S_CTAS_PER_SM = 3;
 constexpr bool L2S_HINTS = true;  // L2 policies: keep a tile between its two loads, drop it after
 
-template <int OP, class T, int PREC, bool R2L>
-__global__ void __launch_bounds__(L2S_THREADS, L2S_CTAS_PER_SM)
-scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a) {
+template <int OP, class T, int PREC, bool R2L, int PROD = 0>
+__global__ void __launch_bounds__(L2S_THREADS, PROD == 2 ? 2 : L2S_CTAS_PER_SM)
+scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a,
+               const __grid_constant__ CUtensorMap tin2) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
@@ -478,6 +505,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
   extern __shared__ unsigned char smem_raw[];
   unsigned char *bufA = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char *bufB = bufA + L2S_TILE;
+  unsigned char *bufY = bufB + L2S_TILE;  // PROD 2: the tile of the second array
   __shared__ uint64_t fullA, fullB, aggr[2], pref[2];
   __shared__ int64_t s_claim;    // dynamic index of the tile pass 1 takes next
   __shared__ int64_t s_tile[2];  // tile in look-back slot p (-1: stop)
@@ -485,6 +513,18 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
   __shared__ S s_agg[2], s_prefix[2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   auto tile_of = [&](int64_t d) { return R2L ? a.ntiles - 1 - d : d; };
+  // pass 1's load of the tile with dynamic index d (thread 0): from HBM, kept in L2
+  auto load_a = [&](int64_t d) {
+    const int row = (int)(tile_of(d) * SCAN_THREADS);
+    mbar_expect_tx(&fullA, PROD == 2 ? 2 * L2S_TILE : L2S_TILE);
+    if constexpr (L2S_HINTS) {
+      tma_load_2d_hint(bufA, &tin, 0, row, &fullA, l2_policy_evict_last());
+      if constexpr (PROD == 2) tma_load_2d_hint(bufY, &tin2, 0, row, &fullA, l2_policy_evict_first());
+    } else {
+      tma_load_2d(bufA, &tin, 0, row, &fullA);
+      if constexpr (PROD == 2) tma_load_2d(bufY, &tin2, 0, row, &fullA);
+    }
+  };
 
   if (tid == 0) {
     mbar_init(&fullA, 1);
@@ -496,13 +536,10 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     fence_mbar_init();
     prefetch_tmap(&tin);
     prefetch_tmap(&tout);
+    if constexpr (PROD == 2) prefetch_tmap(&tin2);
     const int64_t d = (int64_t)atomicAdd(a.ticket, 1u);
     s_claim = d;
-    if (d < a.ntiles) {
-      mbar_expect_tx(&fullA, L2S_TILE);
-      if constexpr (L2S_HINTS) tma_load_2d_hint(bufA, &tin, 0, (int)(tile_of(d) * SCAN_THREADS), &fullA, l2_policy_evict_last());
-      else tma_load_2d(bufA, &tin, 0, (int)(tile_of(d) * SCAN_THREADS), &fullA);
-    }
+    if (d < a.ntiles) load_a(d);
   }
   __syncthreads();
 
@@ -536,6 +573,12 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
   const T idT = Prim<OP, T>::id();
   const T *src = static_cast<const T *>(a.in);
   T *dst = static_cast<T *>(a.out);
+  const T *src2 = static_cast<const T *>(a.in2);
+  const T mapc = from_bits<T>(a.mapc);
+  (void)src2;
+  (void)mapc;
+  // Row `tid` of a tile as the scan sees it: from shared memory for full rows
+  // (PROD 2: already zipped there), else produced from global memory.
   auto load_row = [&](const unsigned char *buf, int64_t tile, T (&x)[ITEMS]) {
     const int64_t grow = tile * SCAN_THREADS + tid;
     if (grow < a.full_rows) {
@@ -544,10 +587,21 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         const uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(tid, c));
         memcpy(&x[c * VEC], &v, 16);
       }
+      if constexpr (PROD == 1) {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) x[j] = zip_elem(a.zop, x[j], mapc);
+      }
     } else {
       const int64_t e0 = grow * ITEMS;
 #pragma unroll
-      for (int j = 0; j < ITEMS; ++j) x[j] = (e0 + j < a.n) ? src[e0 + j] : idT;
+      for (int j = 0; j < ITEMS; ++j) {
+        x[j] = idT;
+        if (e0 + j < a.n) {
+          if constexpr (PROD == 2) x[j] = zip_elem(a.zop, src[e0 + j], src2[e0 + j]);
+          else if constexpr (PROD == 1) x[j] = zip_elem(a.zop, src[e0 + j], mapc);
+          else x[j] = src[e0 + j];
+        }
+      }
     }
   };
   int64_t d_new = s_claim;
@@ -562,11 +616,15 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     int64_t t_new = -1;
     S excl_new = A::id();
     if (t_cur >= 0 && tid == 0) {
-      // the current tile's second load (from L2) runs during the next tile's fold
-      tma_store_wait_read();  // the previous store has read B
+      // the current tile's second load (from L2) runs during the next tile's
+      // fold; PROD 2 reads the zipped tile that pass 1 stored in the output,
+      // once that store is complete
+      if constexpr (PROD == 2) tma_store_wait_all();
+      else tma_store_wait_read();  // the previous store has read B
       mbar_expect_tx(&fullB, L2S_TILE);
-      if constexpr (L2S_HINTS) tma_load_2d_hint(bufB, &tin, 0, (int)(t_cur * SCAN_THREADS), &fullB, l2_policy_evict_first());
-      else tma_load_2d(bufB, &tin, 0, (int)(t_cur * SCAN_THREADS), &fullB);
+      const CUtensorMap *t2 = PROD == 2 ? &tout : &tin;
+      if constexpr (L2S_HINTS) tma_load_2d_hint(bufB, t2, 0, (int)(t_cur * SCAN_THREADS), &fullB, l2_policy_evict_first());
+      else tma_load_2d(bufB, t2, 0, (int)(t_cur * SCAN_THREADS), &fullB);
     }
     if (t_cur >= 0) b_loading = true;
     if (have_new) {
@@ -574,6 +632,17 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       t_new = tile_of(d_new);
       if (named_bar_or<1, L2S_COMPUTE>(!mbar_wait_flagged(&fullA, phA, a.err))) { failed = true; break; }
       phA ^= 1u;
+      if constexpr (PROD == 2) {
+        if (t_new * SCAN_THREADS + tid < a.full_rows) {
+          switch (a.zop) {
+            case ACC_ADD: zip_row<T, ACC_ADD>(bufA, bufY, tid); break;
+            case ACC_MUL: zip_row<T, ACC_MUL>(bufA, bufY, tid); break;
+            case ACC_MIN: zip_row<T, ACC_MIN>(bufA, bufY, tid); break;
+            default: zip_row<T, ACC_MAX>(bufA, bufY, tid); break;
+          }
+        }
+        fence_proxy_async_smem();  // the zipped rows, for pass 1's store of A
+      }
       T x[ITEMS];
       load_row(bufA, t_new, x);
       if (!R2L) {
@@ -604,13 +673,17 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         if (!first) publish<S>(a.status, t_new, a.epoch, 1u, bagg);
         mbar_arrive(&aggr[pn]);
         // the CTA's next tile: its HBM load runs during this tile's look-back
+        if constexpr (PROD == 2) {
+          // the zipped tile goes to its place in the output (for pass 2),
+          // and A must be read by that store before the next tile lands in it
+          if constexpr (L2S_HINTS) tma_store_2d_hint(&tout, 0, (int)(t_new * SCAN_THREADS), bufA, l2_policy_evict_last());
+          else tma_store_2d(&tout, 0, (int)(t_new * SCAN_THREADS), bufA);
+          tma_store_commit();
+          tma_store_wait_read();
+        }
         const int64_t dn = (int64_t)atomicAdd(a.ticket, 1u);
         s_claim = dn;
-        if (dn < a.ntiles) {
-          mbar_expect_tx(&fullA, L2S_TILE);
-          if constexpr (L2S_HINTS) tma_load_2d_hint(bufA, &tin, 0, (int)(tile_of(dn) * SCAN_THREADS), &fullA, l2_policy_evict_last());
-          else tma_load_2d(bufA, &tin, 0, (int)(tile_of(dn) * SCAN_THREADS), &fullA);
-        }
+        if (dn < a.ntiles) load_a(dn);
       }
     } else if (tid == 0) {
       s_tile[pn] = -1;  // no more tiles: the look-back warp stops
@@ -689,25 +762,6 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       *a.ticket = 0u;
       *a.done = 0u;
     }
-  }
-}
-
-// Zip one thread's 128-byte row of the two swizzled tiles into the first:
-// buf[row] = g buf[row] buf2[row], element by element.
-template <class T, int Z>
-__device__ __forceinline__ void zip_row(unsigned char *buf, const unsigned char *buf2, int row) {
-  constexpr int VEC = 16 / sizeof(T);
-#pragma unroll
-  for (int c = 0; c < SCAN_ROW_BYTES / 16; ++c) {
-    uint4 v = *reinterpret_cast<const uint4 *>(buf + swz(row, c));
-    const uint4 w = *reinterpret_cast<const uint4 *>(buf2 + swz(row, c));
-    T x[VEC], y[VEC];
-    memcpy(x, &v, 16);
-    memcpy(y, &w, 16);
-#pragma unroll
-    for (int k = 0; k < VEC; ++k) x[k] = Prim<Z, T>::ap(x[k], y[k]);
-    memcpy(&v, x, 16);
-    *reinterpret_cast<uint4 *>(buf + swz(row, c)) = v;
   }
 }
 
@@ -928,24 +982,28 @@ int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_
 
 // The persistent L2-re-read kernel; *launched false when the array cannot be
 // described by a TMA tensor map or the cooperative grid cannot be placed.
-template <int OP, class T, int PREC, bool R2L>
+template <int OP, class T, int PREC, bool R2L, int PROD = 0>
 int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n, bool has_seed,
-                   bool exclusive, uint64_t seed, cudaStream_t s, bool *launched) {
+                   bool exclusive, uint64_t seed, cudaStream_t s, bool *launched, const T *in2 = nullptr,
+                   int zop = 0, uint64_t mapc = 0) {
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
   *launched = false;
-  CUtensorMap tin, tout;
+  CUtensorMap tin, tout, tin2;
   memset(&tin, 0, sizeof(tin));
   memset(&tout, 0, sizeof(tout));
+  memset(&tin2, 0, sizeof(tin2));
   const int64_t full_rows = n / ITEMS;
   if (full_rows == 0 ||
       !encode_2d(&tin, in, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true) ||
       !encode_2d(&tout, out, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true))
     return ACC_OK;
+  if (PROD == 2 && !encode_2d(&tin2, in2, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true))
+    return ACC_OK;
   const int64_t ntiles = cdiv_h(n, (int64_t)SCAN_THREADS * ITEMS);
   // TMA row coordinates are 32-bit: larger arrays take the other kernels.
   if (ntiles * SCAN_THREADS >= (1ll << 31)) return ACC_OK;
-  const size_t smem = 2 * (size_t)L2S_TILE + 1024;
-  auto kern = scan_l2_kernel<OP, T, PREC, R2L>;
+  const size_t smem = (PROD == 2 ? 3 : 2) * (size_t)L2S_TILE + 1024;
+  auto kern = scan_l2_kernel<OP, T, PREC, R2L, PROD>;
   static std::atomic<uint64_t> attr_done{0};
   smem_attrs_once(kern, (int)smem, attr_done);
   int per_sm = 0;
@@ -969,6 +1027,9 @@ int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   a.has_seed = has_seed;
   a.exclusive = exclusive;
   a.tma_in = a.tma_out = 1;
+  a.in2 = in2;
+  a.zop = zop;
+  a.mapc = mapc;
   int64_t grid = (int64_t)device_info().sms * per_sm;
   if (grid > ntiles) grid = ntiles;
   // A cooperative launch places every CTA at once (or fails): the tiles a CTA
@@ -983,7 +1044,7 @@ int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, tin, tout, a);
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, tin, tout, a, tin2);
   *launched = true;
   return cuda_status(e);
 }
@@ -996,18 +1057,18 @@ template <int OP, class T, int PREC, bool R2L, bool MAP = false>
 int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
                    bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s, int mop = 0,
                    uint64_t mapc = 0) {
-  if constexpr (MAP)
-    return launch_scan_1d_sub<OP, T, PREC, R2L, 2, true>(w, in, out, total_out, seed_out, n, has_seed, exclusive,
-                                                          seed, s, mop, mapc);
   // Arrays of at least four 32 KiB tiles per SM take the persistent
   // L2-re-read kernel (ACC_GB300_SCAN_KERNEL=tile keeps the tile kernel).
   static const bool l2k = !(getenv("ACC_GB300_SCAN_KERNEL") && strcmp(getenv("ACC_GB300_SCAN_KERNEL"), "tile") == 0);
   if (l2k && n * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
     bool launched = false;
-    const int st = launch_scan_l2<OP, T, PREC, R2L>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s,
-                                                    &launched);
+    const int st = launch_scan_l2<OP, T, PREC, R2L, MAP ? 1 : 0>(w, in, out, total_out, seed_out, n, has_seed,
+                                                                 exclusive, seed, s, &launched, nullptr, mop, mapc);
     if (st || launched) return st;
   }
+  if constexpr (MAP)
+    return launch_scan_1d_sub<OP, T, PREC, R2L, 2, true>(w, in, out, total_out, seed_out, n, has_seed, exclusive,
+                                                          seed, s, mop, mapc);
   static const int sub = getenv("ACC_GB300_SCAN_SUB") ? atoi(getenv("ACC_GB300_SCAN_SUB")) : 2;
   if (sub == 2)
     return launch_scan_1d_sub<OP, T, PREC, R2L, 2>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed, s);
@@ -1104,6 +1165,15 @@ int launch_scan_zip_1d(Workspace *w, const T *in, const T *in2, int zop, T *out,
                    encode_2d(&tout, out, sizeof(T), ITEMS, full_rows, SCAN_ROW_BYTES, ITEMS, SCAN_THREADS, true);
   const int64_t ntiles = cdiv_h(n, (int64_t)SCAN_THREADS * ITEMS);
   if (ntiles >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
+  // Arrays of at least four 32 KiB tiles per SM take the persistent
+  // L2-re-read kernel, zipping in its first pass.
+  static const bool l2k = !(getenv("ACC_GB300_SCAN_KERNEL") && strcmp(getenv("ACC_GB300_SCAN_KERNEL"), "tile") == 0);
+  if (tma && l2k && n * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
+    bool launched = false;
+    const int st2 = launch_scan_l2<OP, T, PREC, R2L, 2>(w, in, out, total_out, seed_out, n, has_seed, exclusive, seed,
+                                                        s, &launched, in2, zop);
+    if (st2 || launched) return st2;
+  }
   int st = ws_status(w, (size_t)ntiles * 2);
   if (st) return st;
   ScanArgs a{};

@@ -118,6 +118,16 @@ def test_scan_map_sizes(acc, orc, dev, t, n):
 
 
 @pytest.mark.parametrize("t", MTYPES)
+@pytest.mark.parametrize("d,k", FLAVOURS)
+def test_scan_map_persistent(acc, orc, dev, t, d, k):
+    # more than four 32 KiB tiles per SM: the persistent kernel, which maps
+    # each row as it reads it in both passes
+    n = (1 << 23) + 37
+    run_scan_map(acc, orc, dev, t, "+", "+", (n,), d, k)
+    run_scan_map(acc, orc, dev, t, "min", "*", (n,), d, k)
+
+
+@pytest.mark.parametrize("t", MTYPES)
 @pytest.mark.parametrize("shape", [(3000, 33), (9728, 40), (5, 10_000)])
 def test_scan_map_rows(acc, orc, dev, t, shape):
     # rank 2: one CTA per row, one warp per row (many short rows)

@@ -55,6 +55,18 @@ def test_scan_zipwith_sizes(acc, orc, dev, t, n):
 
 
 @pytest.mark.parametrize("t", ZTYPES)
+@pytest.mark.parametrize("d,k", FLAVOURS)
+def test_scan_zipwith_persistent(acc, orc, dev, t, d, k):
+    # more than four 32 KiB tiles per SM: the persistent kernel, which zips in
+    # its first pass and re-reads the zipped tile from L2 (through the
+    # output); the length is not a whole number of 128-byte rows, so the last
+    # row is zipped from global memory in both passes
+    n = (1 << 23) + 37
+    run_scan_zip(acc, orc, dev, t, "+", "*", (n,), d, k)
+    run_scan_zip(acc, orc, dev, t, "max", "+", (n,), d, k)
+
+
+@pytest.mark.parametrize("t", ZTYPES)
 @pytest.mark.parametrize("shape", [(3000, 33), (9728, 40), (5, 10_000)])
 def test_scan_zipwith_rows(acc, orc, dev, t, shape):
     # rank 2: one CTA per row, one warp per row (many short rows)

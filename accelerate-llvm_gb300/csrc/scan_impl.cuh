@@ -66,6 +66,7 @@ struct ScanArgs {
   const void *in2;   // ZIP kernels: the scanned element i is zop(in[i], in2[i])
   int zop;           // ... MAP kernels: it is zop(in[i], c)
   uint64_t mapc;     // MAP kernels: the constant c (bits of one element)
+  int64_t seg_len;   // segmented (row) scans: the rows' length; a row restarts the scan
 };
 
 __device__ __forceinline__ int swz(int row, int chunk) { return row * SCAN_ROW_BYTES + ((chunk ^ (row & 7)) << 4); }
@@ -487,13 +488,23 @@ __device__ __forceinline__ void zip_row(unsigned char *buf, const unsigned char 
 // place in A and, besides folding, stores the zipped tile to its place in the
 // output, where pass 2 finds it in L2; the zipped array thus costs no DRAM
 // traffic and the CTA needs 96 KiB (two per SM).
+// SEG: the array is `n / seg_len` rows of seg_len >= one 128-byte line
+// (scanl1 / scanr1 over the innermost dimension of a rank-2 array, the
+// reference's scanDim, PTX/CodeGen/Scan.hs:441-611): the scan restarts at
+// each row's first element in scan order.  A thread's line holds at most one
+// such start; states are (restarted, value) pairs combined so that a later
+// part that restarted keeps its own value, so warps, tiles and the look-back
+// see segmented combinations.  A tile that holds a row start publishes its
+// last row's partial sum as an inclusive prefix at once (its successors need
+// nothing before it), and a tile that begins with a row start needs no
+// look-back.
 constexpr int L2S_COMPUTE = SCAN_THREADS;
 constexpr int L2S_THREADS = L2S_COMPUTE + 32;
 constexpr int L2S_TILE = SCAN_THREADS * SCAN_ROW_BYTES;
 constexpr int L2S_CTAS_PER_SM = 3;
 constexpr bool L2S_HINTS = true;  // L2 policies: keep a tile between its two loads, drop it after
 
-template <int OP, class T, int PREC, bool R2L, int PROD = 0>
+template <int OP, class T, int PREC, bool R2L, int PROD = 0, bool SEG = false>
 __global__ void __launch_bounds__(L2S_THREADS, PROD == 2 ? 2 : L2S_CTAS_PER_SM)
 scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a,
                const __grid_constant__ CUtensorMap tin2) {
@@ -511,8 +522,14 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
   __shared__ int64_t s_tile[2];  // tile in look-back slot p (-1: stop)
   __shared__ S s_warp[2][NWARP];
   __shared__ S s_agg[2], s_prefix[2];
+  __shared__ bool s_wflag[2][NWARP], s_aflag[2];  // SEG: the part holds a row start
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   auto tile_of = [&](int64_t d) { return R2L ? a.ntiles - 1 - d : d; };
+  // SEG: part `b` follows part `a` in scan order; the pair's state
+  auto seg_then = [&](bool fa, S sa, bool fb, S sb, bool &f) -> S {
+    f = fa || fb;
+    return fb ? sb : (R2L ? A::comb(sb, sa) : A::comb(sa, sb));
+  };
   // pass 1's load of the tile with dynamic index d (thread 0): from HBM, kept in L2
   auto load_a = [&](int64_t d) {
     const int row = (int)(tile_of(d) * SCAN_THREADS);
@@ -552,12 +569,15 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       const int64_t tile = s_tile[p];
       if (tile < 0) break;
       const bool first = R2L ? (tile == a.ntiles - 1) : (tile == 0);
-      const S prefix = first ? (a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id())
-                             : lookback_prefix<A, R2L, SCAN_LOOKBACK>(a, tile);
+      // SEG: a tile whose first element in scan order starts a row needs no prefix
+      const bool fresh = SEG && (R2L ? ((tile + 1) * (int64_t)L2S_TILE / (int64_t)sizeof(T)) % a.seg_len == 0
+                                     : (tile * (int64_t)L2S_TILE / (int64_t)sizeof(T)) % a.seg_len == 0);
+      const S prefix = (first || fresh) ? (a.has_seed ? A::lift(from_bits<T>(a.seed)) : A::id())
+                                        : lookback_prefix<A, R2L, SCAN_LOOKBACK>(a, tile);
       if (lane == 0) {
         const S bagg = s_agg[p];
         const S inclusive = R2L ? A::comb(bagg, prefix) : A::comb(prefix, bagg);
-        publish<S>(a.status, tile, a.epoch, 2u, inclusive);
+        if (!(SEG && s_aflag[p])) publish<S>(a.status, tile, a.epoch, 2u, inclusive);
         s_prefix[p] = prefix;
         const bool last = R2L ? (tile == 0) : (tile == a.ntiles - 1);
         if (last && a.total_out) *static_cast<T *>(a.total_out) = A::lower(inclusive);
@@ -604,9 +624,19 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       }
     }
   };
+  // SEG: the offset within this thread's line of the row start (in scan
+  // order) of tile t's line, or ITEMS when it has none
+  auto seg_start = [&](int64_t t) -> int {
+    const int64_t e0 = (t * SCAN_THREADS + tid) * (int64_t)ITEMS;
+    const int64_t r0 = e0 % a.seg_len;
+    const int64_t jb = R2L ? a.seg_len - 1 - r0 : (r0 == 0 ? 0 : a.seg_len - r0);
+    return jb < ITEMS ? (int)jb : ITEMS;
+  };
+  (void)seg_start;
   int64_t d_new = s_claim;
   int64_t t_cur = -1;
   S excl_cur = A::id();
+  bool exf_cur = false;
   int64_t k = 0;  // tiles this CTA has taken
   uint32_t phA = 0, phB = 0;
   bool failed = false, b_loading = false;
@@ -615,6 +645,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     const int pn = (int)(k & 1), pc = pn ^ 1;
     int64_t t_new = -1;
     S excl_new = A::id();
+    bool exf_new = false;
     if (t_cur >= 0 && tid == 0) {
       // the current tile's second load (from L2) runs during the next tile's
       // fold; PROD 2 reads the zipped tile that pass 1 stored in the output,
@@ -645,7 +676,43 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       }
       T x[ITEMS];
       load_row(bufA, t_new, x);
-      if (!R2L) {
+      if constexpr (SEG) {
+        // the offset of this line's row start (its last element for R2L), if any
+        const int jb = seg_start(t_new);
+        S agg = A::id();
+        if (!R2L) {
+#pragma unroll
+          for (int j = 0; j < ITEMS; ++j) {
+            if (j == jb) agg = A::id();
+            agg = A::push(agg, x[j]);
+          }
+        } else {
+#pragma unroll
+          for (int j = ITEMS - 1; j >= 0; --j) {
+            if (j == jb) agg = A::id();
+            agg = A::push(agg, x[j]);
+          }
+        }
+        bool f = jb < ITEMS;
+#pragma unroll
+        for (int dd = 1; dd < 32; dd <<= 1) {
+          const S ov = R2L ? shfl_down(agg, dd) : shfl_up(agg, dd);
+          const bool of = R2L ? __shfl_down_sync(0xffffffffu, f, dd) : __shfl_up_sync(0xffffffffu, f, dd);
+          if (R2L ? lane + dd < 32 : lane >= dd) {
+            if (!f) agg = R2L ? A::comb(agg, ov) : A::comb(ov, agg);
+            f = f || of;
+          }
+        }
+        const S ev = R2L ? shfl_down(agg, 1) : shfl_up(agg, 1);
+        const bool ef = R2L ? __shfl_down_sync(0xffffffffu, f, 1) : __shfl_up_sync(0xffffffffu, f, 1);
+        const bool edge = R2L ? lane == 31 : lane == 0;
+        excl_new = edge ? A::id() : ev;
+        exf_new = edge ? false : ef;
+        if (R2L ? lane == 0 : lane == 31) {
+          s_warp[pn][warp] = agg;
+          s_wflag[pn][warp] = f;
+        }
+      } else if (!R2L) {
         S agg = A::lift(x[0]);
 #pragma unroll
         for (int j = 1; j < ITEMS; ++j) agg = A::push(agg, x[j]);
@@ -664,13 +731,27 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       }
       named_bar_sync<1, L2S_COMPUTE>();  // A is read; the warp totals are in place
       if (tid == 0) {
-        S bagg = s_warp[pn][0];
+        S bagg;
+        bool tf = false;
+        if constexpr (SEG) {
+          bagg = A::id();
 #pragma unroll
-        for (int w = 1; w < NWARP; ++w) bagg = A::comb(bagg, s_warp[pn][w]);
+          for (int i = 0; i < NWARP; ++i) {
+            const int w = R2L ? NWARP - 1 - i : i;
+            bagg = seg_then(tf, bagg, s_wflag[pn][w], s_warp[pn][w], tf);
+          }
+        } else {
+          bagg = s_warp[pn][0];
+#pragma unroll
+          for (int w = 1; w < NWARP; ++w) bagg = A::comb(bagg, s_warp[pn][w]);
+        }
         s_agg[pn] = bagg;
+        s_aflag[pn] = tf;
         s_tile[pn] = t_new;
         const bool first = R2L ? (t_new == a.ntiles - 1) : (t_new == 0);
-        if (!first) publish<S>(a.status, t_new, a.epoch, 1u, bagg);
+        // SEG: a tile with a row start knows its inclusive prefix already
+        if (tf) publish<S>(a.status, t_new, a.epoch, 2u, bagg);
+        else if (!first) publish<S>(a.status, t_new, a.epoch, 1u, bagg);
         mbar_arrive(&aggr[pn]);
         // the CTA's next tile: its HBM load runs during this tile's look-back
         if constexpr (PROD == 2) {
@@ -698,13 +779,27 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       phB ^= 1u;
       b_loading = false;
       S inner = A::id();
-      if (!R2L) {
-        for (int w = 0; w < warp; ++w) inner = A::comb(inner, s_warp[pc][w]);
-      } else {
-        for (int w = warp + 1; w < NWARP; ++w) inner = A::comb(inner, s_warp[pc][w]);
-      }
       const S pfx = s_prefix[pc];
-      S run = R2L ? A::comb(A::comb(excl_cur, inner), pfx) : A::comb(pfx, A::comb(inner, excl_cur));
+      S run;
+      int jb = ITEMS;
+      if constexpr (SEG) {
+        bool f = false;
+        if (!R2L) {
+          for (int w = 0; w < warp; ++w) inner = seg_then(f, inner, s_wflag[pc][w], s_warp[pc][w], f);
+        } else {
+          for (int w = NWARP - 1; w > warp; --w) inner = seg_then(f, inner, s_wflag[pc][w], s_warp[pc][w], f);
+        }
+        inner = seg_then(f, inner, exf_cur, excl_cur, f);
+        run = f ? inner : (R2L ? A::comb(inner, pfx) : A::comb(pfx, inner));
+        jb = seg_start(t_cur);
+      } else {
+        if (!R2L) {
+          for (int w = 0; w < warp; ++w) inner = A::comb(inner, s_warp[pc][w]);
+        } else {
+          for (int w = warp + 1; w < NWARP; ++w) inner = A::comb(inner, s_warp[pc][w]);
+        }
+        run = R2L ? A::comb(A::comb(excl_cur, inner), pfx) : A::comb(pfx, A::comb(inner, excl_cur));
+      }
       T x[ITEMS];
       load_row(bufB, t_cur, x);
       const int64_t grow = t_cur * SCAN_THREADS + tid;
@@ -718,6 +813,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         for (int kk = 0; kk < VEC; ++kk) {
           const int q = R2L ? VEC - 1 - kk : kk;
           const int j = c * VEC + q;
+          if (SEG && j == jb) run = A::id();
           if (a.exclusive) { y[q] = A::lower(run); run = A::push(run, x[j]); }
           else { run = A::push(run, x[j]); y[q] = A::lower(run); }
         }
@@ -744,6 +840,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     d_new = s_claim;
     t_cur = t_new;
     excl_cur = excl_new;
+    exf_cur = exf_new;
     ++k;
   }
   if (tid == 0) {
@@ -982,10 +1079,10 @@ int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_
 
 // The persistent L2-re-read kernel; *launched false when the array cannot be
 // described by a TMA tensor map or the cooperative grid cannot be placed.
-template <int OP, class T, int PREC, bool R2L, int PROD = 0>
+template <int OP, class T, int PREC, bool R2L, int PROD = 0, bool SEG = false>
 int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n, bool has_seed,
                    bool exclusive, uint64_t seed, cudaStream_t s, bool *launched, const T *in2 = nullptr,
-                   int zop = 0, uint64_t mapc = 0) {
+                   int zop = 0, uint64_t mapc = 0, int64_t seg_len = 0) {
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
   *launched = false;
   CUtensorMap tin, tout, tin2;
@@ -1003,7 +1100,7 @@ int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   // TMA row coordinates are 32-bit: larger arrays take the other kernels.
   if (ntiles * SCAN_THREADS >= (1ll << 31)) return ACC_OK;
   const size_t smem = (PROD == 2 ? 3 : 2) * (size_t)L2S_TILE + 1024;
-  auto kern = scan_l2_kernel<OP, T, PREC, R2L, PROD>;
+  auto kern = scan_l2_kernel<OP, T, PREC, R2L, PROD, SEG>;
   static std::atomic<uint64_t> attr_done{0};
   smem_attrs_once(kern, (int)smem, attr_done);
   int per_sm = 0;
@@ -1030,6 +1127,7 @@ int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   a.in2 = in2;
   a.zop = zop;
   a.mapc = mapc;
+  a.seg_len = SEG ? seg_len : 1;
   int64_t grid = (int64_t)device_info().sms * per_sm;
   if (grid > ntiles) grid = ntiles;
   // A cooperative launch places every CTA at once (or fails): the tiles a CTA
@@ -1205,6 +1303,18 @@ int launch_scan_zip_1d(Workspace *w, const T *in, const T *in2, int zop, T *out,
   return check_launch();
 }
 
+// scanl1 / scanr1 over the rows of a contiguous [outer x inner] array by the
+// persistent kernel's segmented form (scan_seg.cu, a translation unit of its
+// own); *launched false where it does not apply (operator outside + * min
+// max, rows shorter than a 128-byte line, the array not describable by a TMA
+// tensor map), and the row kernels take the call.
+int scan_rows_seg(Workspace *w, int op, int type, int prec, bool r2l, const void *in, void *out, int64_t outer,
+                  int64_t inner, cudaStream_t s, bool *launched);
+template <class T> constexpr int type_code() {
+  return std::is_same<T, int32_t>::value ? ACC_I32 : std::is_same<T, int64_t>::value ? ACC_I64
+       : std::is_same<T, uint32_t>::value ? ACC_U32 : std::is_same<T, float>::value ? ACC_F32 : ACC_F64;
+}
+
 // Every scan flavour over one array, or (ZIP) over zipWith g in in2 with
 // g = zop, both [outer x inner], or (MAP) over map (\x -> g x c) in with
 // g = zop and c given by its bits `mapc`.
@@ -1244,6 +1354,16 @@ int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, in
                                                       seed, s, zop, mapc);
       return launch_scan_1d<OP, T, PREC, false, MAP>(w, in, out, total_out, seed_out, inner, seeded, exclusive,
                                                      seed, s, zop, mapc);
+    }
+  }
+  if constexpr (!ZIP && !MAP) {
+    // Long scanl1 / scanr1 over rows: one segmented pass over the whole array
+    // (at least four 32 KiB tiles per SM).
+    if (kind == ACC_SCAN_INCLUSIVE && outer * inner * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
+      bool launched = false;
+      const int pc = PREC == 1 ? ACC_PREC_COMPENSATED : (PREC == 2 ? ACC_PREC_FP64ACC : ACC_PREC_PLAIN);
+      const int st = scan_rows_seg(w, OP, type_code<T>(), pc, r2l, in, out, outer, inner, s, &launched);
+      if (st || launched) return st;
     }
   }
   RowScanArgs a{};

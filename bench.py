@@ -11,7 +11,7 @@ seeded synthetic data of the workload's shapes and distributions, generated
 on the device; every input is larger than L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --only scan|fold|permute|stencil|foldseg|batched|dotp|scanzip [--scale S]   (one kernel, small case)
+  python bench.py --only scan|fold|permute|stencil|foldseg|batched|dotp|scanzip|stencil3d|rowscan [--scale S]   (one kernel, small case)
 
 `--impl reference` times the CPU restatement of accelerate-llvm-native (the
 reference's own CPU backend cannot be built here) on all host cores over a
@@ -632,6 +632,8 @@ def run_only(args):
     acc.load()
     name = args.only
     stream = torch.cuda.current_stream()
+    if name == "rowscan":
+        return run_rowscan(torch, acc, args, dev)
     if name == "foldseg":
         off, vals, ivals = make_segments(torch, dev, N_SEG_VALUES // args.scale, N_SEGS // args.scale)
         fn, nbytes = (lambda: acc.fold_seg("+", 0.0, vals, off)), BYTES_FOLDSEG // args.scale
@@ -689,6 +691,33 @@ def run_only(args):
     acc.sync()
     ms = e0.elapsed_time(e1) / args.steps
     return {"only": name, "scale": args.scale, "ms": round(ms, 4), "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1)}
+
+
+def run_rowscan(torch, acc, args, dev):
+    """scanl1 (+) over the rows of Int64 arrays of 2^28 / scale elements in
+    four shapes (long rows to many short ones), 16 B per element (read +
+    write), `--steps` calls each after `--warmup`."""
+    total = (1 << 28) // args.scale
+    res = {"only": "rowscan", "scale": args.scale, "shapes": {}}
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 12)
+    x = torch.randint(-(1 << 20), 1 << 20, (total,), dtype=torch.int64, device=dev, generator=g)
+    stream = torch.cuda.current_stream()
+    for inner in (1 << 14, 1 << 18, 1 << 10, 1 << 8):
+        xs = x.view(total // inner, inner)
+        for _ in range(max(1, args.warmup)):
+            acc.scanl1("+", xs)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            acc.scanl1("+", xs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res["shapes"][f"{total // inner}x{inner}"] = {"ms": round(ms, 4), "gbs": round(16 * total / (ms * 1e-3) / 1e9, 1)}
+    acc.sync()
+    return res
 
 
 def link_rates(torch, dev, nbytes=1 << 30, trials=5):
@@ -1024,7 +1053,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="length of the 20k req/s serving stream (0: skip serving)")
     ap.add_argument("--only", choices=["scan", "fold", "permute", "stencil", "foldseg", "batched", "dotp", "scanzip",
-                                       "stencil3d"],
+                                       "stencil3d", "rowscan"],
                     help="time one skeleton alone (small-case driver for ncu captures)")
     ap.add_argument("--scale", type=int, default=1, help="with --only: 1/scale of the full input")
     args = ap.parse_args()

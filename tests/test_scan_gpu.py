@@ -106,6 +106,21 @@ def test_scan_many_short_rows(acc, orc, dev, t, op, shape):
         run_scan(acc, orc, dev, t, op, shape, d, k)
 
 
+# scanl1 / scanr1 over rows of arrays of at least four 32 KiB tiles per SM:
+# one segmented pass of the persistent kernel over the whole array.  Rows
+# longer than a tile (look-backs within a row), rows a whole number of tiles
+# long (tiles that begin with a row: no look-back), many rows per tile, and
+# row lengths that are not a whole number of 128-byte lines (a row start in
+# the middle of a thread's line).
+@pytest.mark.parametrize("t,op,shape", [("i64", "+", (64, 1 << 18)), ("i64", "+", (1 << 16, 256)),
+                                        ("i64", "max", (1024, 1 << 14)), ("i32", "+", (160_000, 37)),
+                                        ("f32", "+", (1000, 5003)), ("f64", "min", (4097, 1000)),
+                                        ("i32", "*", (2000, 4099)), ("u32", "max", (3, 2_000_003))])
+def test_scan_rows_segmented(acc, orc, dev, t, op, shape):
+    for d in (0, 1):
+        run_scan(acc, orc, dev, t, op, shape, d, 0)
+
+
 @pytest.mark.parametrize("offset", [1, 3])
 @pytest.mark.parametrize("t,op", [("i32", "+"), ("i64", "+"), ("f32", "+")])
 def test_scan_unaligned(acc, orc, dev, t, op, offset):

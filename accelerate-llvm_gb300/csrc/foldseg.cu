@@ -489,19 +489,22 @@ foldseg_tile_kernel(const __grid_constant__ CUtensorMap tin, SegTileArgs a) {
     s_bm[tid] = bm;
     s_base[tid] = pbase;
     int pk = pbase;
-#pragma unroll 1
+    // fully unrolled: every mask bit is tested at a constant position
+    const uint32_t bm_lo = (uint32_t)bm, bm_hi = (uint32_t)(bm >> 32);
+    const int r0 = FT_RPT * tid;
+#pragma unroll
     for (int c = 0; c < W / VEC; ++c) {
-      const int r = FT_RPT * tid + c / (ITEMS / VEC);
+      const int r = r0 + c / (ITEMS / VEC);
       const int cc = c % (ITEMS / VEC);
       const int rr = r % FT_THREADS;
       const uint4 v = *reinterpret_cast<const uint4 *>(buf + (r / FT_THREADS) * SUB_BYTES + rr * FT_ROW_BYTES +
                                                        ((cc ^ (rr & 7)) << 4));
       T x[VEC];
       memcpy(x, &v, 16);
-      const uint32_t cb = (uint32_t)(bm >> (c * VEC)) & ((1u << VEC) - 1u);
 #pragma unroll
       for (int q = 0; q < VEC; ++q) {
-        const bool bnd = (cb >> q) & 1u;
+        const int bit = c * VEC + q;
+        const bool bnd = ((bit < 32 ? bm_lo : bm_hi) >> (bit & 31)) & 1u;
         if (bnd) s_res[pk] = acc;
         pk += bnd ? 1 : 0;
         acc = bnd ? A::id() : acc;

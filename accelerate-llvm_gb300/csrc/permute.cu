@@ -301,9 +301,12 @@ __global__ void __launch_bounds__(1024, 1) permute_split(PermArgs a, int per) {
 
 // Histogram (+ of a small positive constant) with 16-bit counters packed two
 // to a word, so 2^16 bins fit in one CTA's shared memory and every update is
-// local.  A counter that wraps is repaired exactly: the carry that ran into
-// the neighbouring counter is taken back and 65536 is added to the target bin
-// in global memory.
+// local.  Word w holds bin w (low half) and bin w + half (high half), half =
+// ceil(m / 2): neighbouring bins, which skewed (Zipf-like) indices make hot
+// together, sit in different words and banks, so their updates do not
+// serialise on one address.  A counter that wraps is repaired exactly: the
+// carry that ran into the word's other counter is taken back and 65536 is
+// added to the target bin in global memory.
 template <bool AGG>
 __global__ void __launch_bounds__(1024, 1) permute_hist16(PermArgs a) {
   extern __shared__ __align__(16) uint32_t words[];
@@ -330,11 +333,12 @@ __global__ void __launch_bounds__(1024, 1) permute_hist16(PermArgs a) {
     // a counter is one atomic whose returned old word shows the crossing:
     //  * an update of bin j crosses when old16 + inc > 0xffff;
     //  * a low counter that crosses also carries +1 into the high counter
-    //    (a crossing for bin j+1 when the old high half was 0xffff), and the
-    //    carry is then taken back with -1 (a crossing back when the high half
-    //    it finds is 0).  Accounting for all three keeps every bin exact.
-    const uint32_t wi = (uint32_t)j >> 1;
-    const uint32_t sh = ((uint32_t)j & 1u) * 16u;
+    //    (a crossing for bin j+half when the old high half was 0xffff), and
+    //    the carry is then taken back with -1 (a crossing back when the high
+    //    half it finds is 0).  Accounting for all three keeps every bin exact.
+    const bool low = (uint32_t)j < nwords;
+    const uint32_t wi = low ? (uint32_t)j : (uint32_t)j - nwords;
+    const uint32_t sh = low ? 0u : 16u;
     const uint32_t old = atomicAdd(&words[wi], inc << sh);
     if (((old >> sh) & 0xffffu) + inc > 0xffffu) {
       atomicAdd(out + j, 65536u);
@@ -342,7 +346,7 @@ __global__ void __launch_bounds__(1024, 1) permute_hist16(PermArgs a) {
         int d = (old >> 16) == 0xffffu ? 1 : 0;
         const uint32_t old2 = atomicSub(&words[wi], 1u << 16);
         d -= (old2 >> 16) == 0u ? 1 : 0;
-        if (d != 0 && (uint32_t)j + 1 < m) atomicAdd(out + j + 1, (uint32_t)(d * 65536));
+        if (d != 0 && (uint32_t)j + nwords < m) atomicAdd(out + j + nwords, (uint32_t)(d * 65536));
       }
     }
   };
@@ -369,8 +373,8 @@ __global__ void __launch_bounds__(1024, 1) permute_hist16(PermArgs a) {
   __syncthreads();
   for (uint32_t b = threadIdx.x; b < nwords; b += blockDim.x) {
     const uint32_t w = words[b];
-    if (w & 0xffffu) atomicAdd(out + 2 * b, w & 0xffffu);
-    if ((w >> 16) && 2 * b + 1 < m) atomicAdd(out + 2 * b + 1, w >> 16);
+    if (w & 0xffffu) atomicAdd(out + b, w & 0xffffu);
+    if ((w >> 16) && b + nwords < m) atomicAdd(out + b + nwords, w >> 16);
   }
 }
 

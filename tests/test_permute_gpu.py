@@ -90,14 +90,18 @@ def test_permute_empty(acc, dev):
 
 
 @pytest.mark.parametrize("c", [1, 7, 2047])
-def test_permute_histogram_counter_wrap(acc, orc, dev, c):
-    # Two adjacent hot bins (one packed word) take most of 2^25 updates, so the
-    # per-CTA 16-bit counters wrap many times, concurrently with the carries.
+@pytest.mark.parametrize("m,pair", [(1 << 16, (2, 3)), (1 << 16, (5, 5 + (1 << 15))), (65535, (9, 9 + 32768))])
+def test_permute_histogram_counter_wrap(acc, orc, dev, c, m, pair):
+    # Two hot bins take most of 2^25 updates, so the per-CTA 16-bit counters
+    # wrap many times: neighbouring bins (different packed words), and the two
+    # bins of one packed word (bin w and bin w + ceil(m / 2)), whose low
+    # counter's carries run into the high one concurrently with its own
+    # updates; an odd bin count leaves the last word's high half unused.
     rng = np.random.default_rng(c)
-    n, m = 1 << 25, 1 << 16
+    n = 1 << 25
     idx = rng.integers(0, m, size=n).astype(np.int32)
     hot = rng.random(n) < 0.9
-    idx[hot] = rng.integers(0, 2, size=int(hot.sum())).astype(np.int32) + 2
+    idx[hot] = np.array(pair, dtype=np.int32)[rng.integers(0, 2, size=int(hot.sum()))]
     got = acc.permute("+", torch.zeros(m, dtype=torch.int32, device=dev), torch.from_numpy(idx).to(dev), c)
     acc.sync()
     ref = (np.bincount(idx, minlength=m).astype(np.int64) * c).astype(np.uint32).view(np.int32)

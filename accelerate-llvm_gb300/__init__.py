@@ -605,7 +605,8 @@ class Batch:
 
 
 def batch_autotune(table_path=None, stream=None):
-    """Run the batch tile-size autotuner (acc_batch_autotune)."""
+    """Run the batch autotuner (acc_batch_autotune): threads per CTA and
+    elements per thread per (kind, type, size bucket)."""
     _check(lib().acc_batch_autotune(table_path.encode() if table_path else None, _stream(stream)), "autotune")
 
 

@@ -4,8 +4,10 @@
 // The reference launches every skeleton separately, each with host-side
 // set-up (PTX/Execute.hs:835-881); thousands of small and medium requests are
 // dominated by launch latency.  Here a plan flattens a batch into work items
-// (request, tile), each request cut into tiles of 256 x IPT elements, IPT
-// chosen per (kind, type, size bucket) by the autotuner.  One persistent
+// (request, tile), each request cut into tiles of NT x IPT elements; the
+// autotuner picks the launch shape (NT threads per CTA: 128, 256 or 512) and
+// the tile shape (IPT elements per thread) per (kind, type, size bucket), and
+// a batch runs with the NT preferred by most of its bytes.  One persistent
 // kernel draws items from an atomic ticket in table order:
 //   * fold tiles reduce their chunk (16-byte vector loads); the last tile of
 //     a request (per-request atomic ticket) folds the tile partials in order
@@ -32,7 +34,7 @@
 
 namespace accgb {
 
-constexpr int BT = 256;                    // threads per CTA
+constexpr int BT = 256;                    // threads per CTA of untuned launches and of the serving arena
 constexpr int B_MAX_TILE_BYTES = 32768;    // largest tile staged in shared memory
 
 struct BReq {
@@ -78,28 +80,28 @@ __device__ __forceinline__ uint32_t b_peek(const uint64_t *status, int64_t t, ui
 }
 
 // CTA-wide ordered reduction (valid in thread 0).
-template <class A>
+template <class A, int NT>
 __device__ __forceinline__ typename A::S b_block_reduce(typename A::S v, typename A::S *s_part) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   v = warp_reduce<A>(v);
   if (lane == 0) s_part[warp] = v;
   __syncthreads();
   if (warp == 0) {
-    v = lane < BT / 32 ? s_part[lane] : A::id();
+    v = lane < NT / 32 ? s_part[lane] : A::id();
     v = warp_reduce<A>(v);
   }
   __syncthreads();
   return v;
 }
 
-template <int OP, class T, int PREC>
+template <int OP, class T, int PREC, int NT>
 __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int32_t r, unsigned char *smem) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
   __shared__ bool s_last;
   S *s_part = reinterpret_cast<S *>(smem);
   const int64_t tile = item - q.first_item;
-  const int64_t ts = (int64_t)q.ipt * BT;
+  const int64_t ts = (int64_t)q.ipt * NT;
   const int64_t b = tile * ts;
   const int64_t e = b + ts < q.n ? b + ts : q.n;
   const T *src = static_cast<const T *>(q.in) + b;
@@ -113,7 +115,7 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
   if ((int64_t)threadIdx.x < head) acc = A::push(acc, src[threadIdx.x]);
   const int64_t nvec = (len - head) / VEC;
   const uint4 *qv = reinterpret_cast<const uint4 *>(src + head);
-  for (int64_t i = threadIdx.x; i < nvec; i += BT) {
+  for (int64_t i = threadIdx.x; i < nvec; i += NT) {
     uint4 v = ld_stream16(qv + i);
     T el[VEC];
     memcpy(el, &v, 16);
@@ -122,7 +124,7 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
   }
   const int64_t tail0 = head + nvec * VEC;
   if (tail0 + threadIdx.x < len) acc = A::push(acc, src[tail0 + threadIdx.x]);
-  acc = b_block_reduce<A>(acc, s_part);
+  acc = b_block_reduce<A, NT>(acc, s_part);
   // One 8-byte slot per item whatever the state's size, so that requests of
   // different types in one batch never share partial slots.
   static_assert(sizeof(S) <= sizeof(uint64_t), "fold state larger than a partial slot");
@@ -137,10 +139,10 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
   if (s_last) {
     __threadfence();
     S v = A::id();
-    const int64_t per = (q.ntiles + BT - 1) / BT;
+    const int64_t per = (q.ntiles + NT - 1) / NT;
     const int64_t lo = threadIdx.x * per, hi = lo + per < q.ntiles ? lo + per : q.ntiles;
     for (int64_t i = lo; i < hi; ++i) v = A::comb(v, ld_state<S>(part(q.first_item + i)));
-    v = b_block_reduce<A>(v, s_part);
+    v = b_block_reduce<A, NT>(v, s_part);
     if (threadIdx.x == 0) {
       if (q.has_seed) v = A::comb(A::lift(from_bits<T>(q.seed)), v);
       *static_cast<T *>(q.out) = A::lower(v);
@@ -150,22 +152,22 @@ __device__ void b_fold_tile(const BatchArgs &a, const BReq &q, int64_t item, int
   __syncthreads();
 }
 
-template <int OP, class T, int PREC, int IPT>
+template <int OP, class T, int PREC, int IPT, int NT>
 __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uint32_t epoch, unsigned char *smem) {
   using A = Acc<OP, T, PREC>;
   using S = typename A::S;
-  __shared__ S s_warp[BT / 32];
+  __shared__ S s_warp[NT / 32];
   __shared__ S s_prefix;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int ipt = IPT;  // compile time: the staging index math is shifts and masks
   constexpr int pitch = ipt + 1;  // padded row: conflict-free thread-per-row access
   T *tile_s = reinterpret_cast<T *>(smem + 256);
   const int64_t tile = item - q.first_item;
-  const int64_t ts = (int64_t)ipt * BT;
+  const int64_t ts = (int64_t)ipt * NT;
   const int64_t b = tile * ts;
   const T idT = Prim<OP, T>::id();
   const T *src = static_cast<const T *>(q.in);
-  for (int k = tid; k < ts; k += BT) {
+  for (int k = tid; k < ts; k += NT) {
     const int64_t gi = b + k;
     tile_s[(k / ipt) * pitch + (k % ipt)] = gi < q.n ? src[gi] : idT;
   }
@@ -183,7 +185,7 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
   for (int w = 0; w < warp; ++w) wpre = A::comb(wpre, s_warp[w]);
   if (warp == 0) {
     S bagg = s_warp[0];
-    for (int w = 1; w < BT / 32; ++w) bagg = A::comb(bagg, s_warp[w]);
+    for (int w = 1; w < NT / 32; ++w) bagg = A::comb(bagg, s_warp[w]);
     S prefix = q.has_seed ? A::lift(from_bits<T>(q.seed)) : A::id();
     if (tile > 0) {
       if (lane == 0) b_publish<S>(a.status, item, epoch, 1u, bagg);
@@ -239,7 +241,7 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
   }
   __syncthreads();
   T *dst = static_cast<T *>(q.out);
-  for (int k = tid; k < ts; k += BT) {
+  for (int k = tid; k < ts; k += NT) {
     const int64_t gi = b + k;
     if (gi < q.n) dst[gi] = tile_s[(k / ipt) * pitch + (k % ipt)];
   }
@@ -247,28 +249,35 @@ __device__ void b_scan_tile(const BatchArgs &a, const BReq &q, int64_t item, uin
 }
 
 // Scan tiles are instantiated per elements-per-thread (powers of two up to
-// the 32 KiB tile limit), picked by the tile's planned value.
-template <int OP, class T, int PREC>
+// the 32 KiB tile limit for NT threads), picked by the tile's planned value.
+template <int OP, class T, int PREC, int NT>
 __device__ __forceinline__ void b_scan_tile_any(const BatchArgs &a, const BReq &q, int64_t item, uint32_t epoch,
                                                 unsigned char *smem) {
+  constexpr int MAXI = B_MAX_TILE_BYTES / (NT * (int)sizeof(T));
   switch (q.ipt) {
-    case 1: b_scan_tile<OP, T, PREC, 1>(a, q, item, epoch, smem); break;
-    case 2: b_scan_tile<OP, T, PREC, 2>(a, q, item, epoch, smem); break;
-    case 4: b_scan_tile<OP, T, PREC, 4>(a, q, item, epoch, smem); break;
-    case 8: b_scan_tile<OP, T, PREC, 8>(a, q, item, epoch, smem); break;
+    case 1: b_scan_tile<OP, T, PREC, 1, NT>(a, q, item, epoch, smem); break;
+    case 2: b_scan_tile<OP, T, PREC, 2, NT>(a, q, item, epoch, smem); break;
+    case 4: b_scan_tile<OP, T, PREC, 4, NT>(a, q, item, epoch, smem); break;
+    case 8: b_scan_tile<OP, T, PREC, 8, NT>(a, q, item, epoch, smem); break;
     default:
-      if constexpr (sizeof(T) == 4) {
-        if (q.ipt == 32) { b_scan_tile<OP, T, PREC, 32>(a, q, item, epoch, smem); break; }
+      if constexpr (MAXI >= 64) {
+        if (q.ipt == 64) { b_scan_tile<OP, T, PREC, 64, NT>(a, q, item, epoch, smem); break; }
       }
-      b_scan_tile<OP, T, PREC, 16>(a, q, item, epoch, smem);
+      if constexpr (MAXI >= 32) {
+        if (q.ipt == 32) { b_scan_tile<OP, T, PREC, 32, NT>(a, q, item, epoch, smem); break; }
+      }
+      if constexpr (MAXI >= 16) b_scan_tile<OP, T, PREC, 16, NT>(a, q, item, epoch, smem);
+      else b_scan_tile<OP, T, PREC, 8, NT>(a, q, item, epoch, smem);
       break;
   }
 }
 
 enum { BK_FOLD = 0, BK_SCAN = 1 };
 
-template <int OP>
-__global__ void __launch_bounds__(BT, 5) batch_kernel(BatchArgs a) {
+// The register budget: ~51 per thread with 256 or 512 threads (1,280 threads
+// per SM), 64 with 128 threads (1,024 per SM; 48 would spill).
+template <int OP, int NT>
+__global__ void __launch_bounds__(NT, NT == 128 ? 8 : 1280 / NT) batch_kernel(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int64_t s_item;
   __shared__ BReq s_req;
@@ -295,17 +304,17 @@ __global__ void __launch_bounds__(BT, 5) batch_kernel(BatchArgs a) {
     const uint32_t epoch = s_epoch;
     if (q.kind == BK_FOLD) {
       switch (q.type) {
-        case ACC_I32: b_fold_tile<OP, int32_t, 0>(a, q, item, r, smem); break;
-        case ACC_I64: b_fold_tile<OP, int64_t, 0>(a, q, item, r, smem); break;
-        case ACC_F32: b_fold_tile<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN>(a, q, item, r, smem); break;
-        default: b_fold_tile<OP, double, 0>(a, q, item, r, smem); break;
+        case ACC_I32: b_fold_tile<OP, int32_t, 0, NT>(a, q, item, r, smem); break;
+        case ACC_I64: b_fold_tile<OP, int64_t, 0, NT>(a, q, item, r, smem); break;
+        case ACC_F32: b_fold_tile<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN, NT>(a, q, item, r, smem); break;
+        default: b_fold_tile<OP, double, 0, NT>(a, q, item, r, smem); break;
       }
     } else {
       switch (q.type) {
-        case ACC_I32: b_scan_tile_any<OP, int32_t, 0>(a, q, item, epoch, smem); break;
-        case ACC_I64: b_scan_tile_any<OP, int64_t, 0>(a, q, item, epoch, smem); break;
-        case ACC_F32: b_scan_tile_any<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN>(a, q, item, epoch, smem); break;
-        default: b_scan_tile_any<OP, double, 0>(a, q, item, epoch, smem); break;
+        case ACC_I32: b_scan_tile_any<OP, int32_t, 0, NT>(a, q, item, epoch, smem); break;
+        case ACC_I64: b_scan_tile_any<OP, int64_t, 0, NT>(a, q, item, epoch, smem); break;
+        case ACC_F32: b_scan_tile_any<OP, float, OP == ACC_ADD ? PREC_COMP : PREC_PLAIN, NT>(a, q, item, epoch, smem); break;
+        default: b_scan_tile_any<OP, double, 0, NT>(a, q, item, epoch, smem); break;
       }
     }
     __syncthreads();
@@ -313,22 +322,28 @@ __global__ void __launch_bounds__(BT, 5) batch_kernel(BatchArgs a) {
 }
 
 // ---------------------------------------------------------------- autotuner table
-// Elements per thread (IPT) per (kind, type, log2 size bucket); the tile is
-// 256 x IPT elements.  Filled by acc_batch_autotune, persisted as JSON.
+// Launch and tile shape per (kind, type, log2 size bucket): NT threads per CTA
+// and IPT elements per thread (a tile is NT x IPT elements).  Filled by
+// acc_batch_autotune, persisted as JSON.
+constexpr int B_NT[3] = {128, 256, 512};
 struct TuneKey {
   int kind, type, bucket;
   bool operator<(const TuneKey &o) const { return std::tie(kind, type, bucket) < std::tie(o.kind, o.type, o.bucket); }
 };
+struct TuneVal {
+  int ipt, nt;
+};
 static std::mutex g_tune_mu;
-static std::map<TuneKey, int> g_tune;
+static std::map<TuneKey, TuneVal> g_tune;
 
+static bool valid_nt(int nt) { return nt == 128 || nt == 256 || nt == 512; }
 static int type_bytes(int type) { return (type == ACC_I64 || type == ACC_F64) ? 8 : 4; }
-static int max_ipt(int type) { return B_MAX_TILE_BYTES / (BT * type_bytes(type)); }
+static int max_ipt(int type, int nt) { return B_MAX_TILE_BYTES / (nt * type_bytes(type)); }
 // Elements per thread as the kernel takes them: within [1, max_ipt], rounded
 // down to a power of two (scan tiles are instantiated for those only).
-static int norm_ipt(int ipt, int type) {
+static int norm_ipt(int ipt, int type, int nt) {
   if (ipt < 1) ipt = 1;
-  if (ipt > max_ipt(type)) ipt = max_ipt(type);
+  if (ipt > max_ipt(type, nt)) ipt = max_ipt(type, nt);
   int p = 1;
   while (p * 2 <= ipt) p *= 2;
   return p;
@@ -339,17 +354,26 @@ static int bucket_of(int64_t n) {
   return b;
 }
 static int default_ipt(int kind, int type, int64_t n) {
-  // Before tuning: one wave of small tiles for small requests, large tiles otherwise.
-  const int cap = max_ipt(type);
+  // Before tuning (256 threads): one wave of small tiles for small requests,
+  // large tiles otherwise.
+  const int cap = max_ipt(type, BT);
   int ipt = n <= (1 << 14) ? 4 : n <= (1 << 18) ? 8 : 16;
   (void)kind;
   return ipt < cap ? ipt : cap;
 }
-static int tuned_ipt(int kind, int type, int64_t n) {
+static TuneVal tuned(int kind, int type, int64_t n) {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tune.find(TuneKey{kind, type, bucket_of(n)});
   if (it != g_tune.end()) return it->second;
-  return default_ipt(kind, type, n);
+  return TuneVal{default_ipt(kind, type, n), BT};
+}
+// A request's elements per thread in a launch of nt threads: its tuned tile
+// shape where the tuned launch shape is nt, else the same tile size in
+// elements.
+static int ipt_for(const acc_request &q, int nt) {
+  const TuneVal v = tuned(q.kind, q.type, q.n);
+  const int ipt = v.nt == nt ? v.ipt : (int)(((int64_t)v.ipt * v.nt) / nt);
+  return norm_ipt(ipt, q.type, nt);
 }
 
 // ---------------------------------------------------------------- plan
@@ -364,19 +388,33 @@ struct Batch {
   uint32_t *d_req_ticket = nullptr;
   uint32_t *d_words = nullptr;
   int grid = 0;
+  int nt = BT;  // threads per CTA
   size_t smem = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
 
-template <int OP> static void *batch_kernel_ptr() { return reinterpret_cast<void *>(batch_kernel<OP>); }
+template <int OP> static void *batch_kernel_ptr(int nt) {
+  if (nt == 128) return reinterpret_cast<void *>(batch_kernel<OP, 128>);
+  if (nt == 512) return reinterpret_cast<void *>(batch_kernel<OP, 512>);
+  return reinterpret_cast<void *>(batch_kernel<OP, 256>);
+}
+static void *kernel_for(int op, int nt) {
+  return op == ACC_ADD ? batch_kernel_ptr<ACC_ADD>(nt) : op == ACC_MIN ? batch_kernel_ptr<ACC_MIN>(nt)
+                                                                       : batch_kernel_ptr<ACC_MAX>(nt);
+}
 
+template <int OP> static void launch_op(Batch *b, const BatchArgs &a, cudaStream_t s) {
+  if (b->nt == 128) batch_kernel<OP, 128><<<b->grid, 128, b->smem, s>>>(a);
+  else if (b->nt == 512) batch_kernel<OP, 512><<<b->grid, 512, b->smem, s>>>(a);
+  else batch_kernel<OP, 256><<<b->grid, 256, b->smem, s>>>(a);
+}
 static int batch_launch_raw(Batch *b, cudaStream_t s) {
   BatchArgs a{b->d_reqs, b->d_item_req, b->nitems, b->d_status, b->d_partials, b->d_req_ticket, b->d_words};
   switch (b->op) {
-    case ACC_ADD: batch_kernel<ACC_ADD><<<b->grid, BT, b->smem, s>>>(a); break;
-    case ACC_MIN: batch_kernel<ACC_MIN><<<b->grid, BT, b->smem, s>>>(a); break;
-    default: batch_kernel<ACC_MAX><<<b->grid, BT, b->smem, s>>>(a); break;
+    case ACC_ADD: launch_op<ACC_ADD>(b, a, s); break;
+    case ACC_MIN: launch_op<ACC_MIN>(b, a, s); break;
+    default: launch_op<ACC_MAX>(b, a, s); break;
   }
   return check_launch();
 }
@@ -394,9 +432,29 @@ static void batch_free(Batch *b) {
   delete b;
 }
 
-static int batch_make(int op, const acc_request *reqs, int64_t count, const int32_t *ipt_override, Batch **out) {
+// nt_override > 0 fixes the launch shape (with ipt_override, the tile
+// shapes: the autotuner's trial launches); otherwise the batch takes the
+// tuned launch shape that most of its bytes prefer.
+static int batch_make(int op, const acc_request *reqs, int64_t count, const int32_t *ipt_override, int nt_override,
+                      Batch **out) {
   if (op != ACC_ADD && op != ACC_MIN && op != ACC_MAX) return ACC_ERR_UNSUPPORTED;
   if (count < 0 || (count > 0 && !reqs) || count > (1ll << 31) - 1) return ACC_ERR_INVALID;
+  int nt = BT;
+  if (nt_override > 0) {
+    if (!valid_nt(nt_override)) return ACC_ERR_INVALID;
+    nt = nt_override;
+  } else {
+    double weight[3] = {0.0, 0.0, 0.0};
+    for (int64_t i = 0; i < count; ++i) {
+      const acc_request &q = reqs[i];
+      if (q.type != ACC_I32 && q.type != ACC_I64 && q.type != ACC_F32 && q.type != ACC_F64) continue;
+      const int v = tuned(q.kind, q.type, q.n).nt;
+      for (int c = 0; c < 3; ++c)
+        if (B_NT[c] == v) weight[c] += (double)(q.n > 0 ? q.n : 0) * type_bytes(q.type);
+    }
+    if (weight[0] > weight[1] && weight[0] >= weight[2]) nt = B_NT[0];
+    else if (weight[2] > weight[1] && weight[2] > weight[0]) nt = B_NT[2];
+  }
   std::vector<BReq> h(count);
   std::vector<int32_t> item_req;
   int64_t nitems = 0;
@@ -408,22 +466,23 @@ static int batch_make(int op, const acc_request *reqs, int64_t count, const int3
     if (q.n < 0 || (q.n > 0 && (!q.in || !q.out))) return ACC_ERR_INVALID;
     if (q.kind == ACC_REQ_FOLD && !q.out) return ACC_ERR_INVALID;  // fold z [] still writes z
     if (q.kind == ACC_REQ_FOLD && q.n == 0 && !q.has_seed) return ACC_ERR_EMPTY;
-    const int ipt = norm_ipt(ipt_override ? ipt_override[i] : tuned_ipt(q.kind, q.type, q.n), q.type);
-    const int64_t ts = (int64_t)ipt * BT;
-    int64_t nt = (q.n + ts - 1) / ts;
-    if (q.kind == ACC_REQ_FOLD && nt == 0) nt = 1;  // fold z [] = z: one (empty) tile writes the seed
+    const int ipt = ipt_override ? norm_ipt(ipt_override[i], q.type, nt) : ipt_for(q, nt);
+    const int64_t ts = (int64_t)ipt * nt;
+    int64_t ntl = (q.n + ts - 1) / ts;
+    if (q.kind == ACC_REQ_FOLD && ntl == 0) ntl = 1;  // fold z [] = z: one (empty) tile writes the seed
     BReq &r = h[i];
     r.in = q.in; r.out = q.out; r.n = q.n; r.seed = q.seed;
     r.kind = q.kind; r.type = q.type; r.has_seed = q.has_seed; r.ipt = ipt;
-    r.first_item = nitems; r.ntiles = nt;
-    for (int64_t k = 0; k < nt; ++k) item_req.push_back((int32_t)i);
-    nitems += nt;
-    const size_t tb = (size_t)(ipt + 1) * BT * type_bytes(q.type) + 256;
+    r.first_item = nitems; r.ntiles = ntl;
+    for (int64_t k = 0; k < ntl; ++k) item_req.push_back((int32_t)i);
+    nitems += ntl;
+    const size_t tb = (size_t)(ipt + 1) * nt * type_bytes(q.type) + 256;
     if (tb > max_tile) max_tile = tb;
   }
   if (nitems >= (1ll << 31)) return ACC_ERR_TOO_LARGE;
   Batch *b = new Batch();
   b->op = op;
+  b->nt = nt;
   cudaGetDevice(&b->device);
   b->count = count;
   b->nitems = nitems;
@@ -441,11 +500,10 @@ static int batch_make(int op, const acc_request *reqs, int64_t count, const int3
   cudaMemset(b->d_status, 0, sizeof(uint64_t) * 2 * (nitems ? nitems : 1));
   cudaMemset(b->d_req_ticket, 0, sizeof(uint32_t) * (count ? count : 1));
   cudaMemset(b->d_words, 0, sizeof(uint32_t) * 64);
-  void *kern = op == ACC_ADD ? batch_kernel_ptr<ACC_ADD>() : op == ACC_MIN ? batch_kernel_ptr<ACC_MIN>()
-                                                                          : batch_kernel_ptr<ACC_MAX>();
+  void *kern = kernel_for(op, nt);
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, b->smem) != cudaSuccess || per_sm < 1) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, nt, b->smem) != cudaSuccess || per_sm < 1) {
     cudaGetLastError();
     per_sm = 1;
   }
@@ -495,8 +553,8 @@ int arena_create(int op, int64_t cap_reqs, int64_t cap_items, BatchArena **out) 
   cudaMemset(b->d_req_ticket, 0, sizeof(uint32_t) * cap_reqs);
   cudaMemset(b->d_words, 0, sizeof(uint32_t) * 64);
   b->smem = (size_t)B_MAX_TILE_BYTES + BT * 8 + 256;
-  void *kern = op == ACC_ADD ? batch_kernel_ptr<ACC_ADD>() : op == ACC_MIN ? batch_kernel_ptr<ACC_MIN>()
-                                                                          : batch_kernel_ptr<ACC_MAX>();
+  b->nt = BT;
+  void *kern = kernel_for(op, BT);
   cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BT, b->smem) != cudaSuccess || per_sm < 1) {
@@ -512,7 +570,7 @@ int arena_create(int op, int64_t cap_reqs, int64_t cap_items, BatchArena **out) 
 
 // Tiles a request will take (0 if it does not fit the batch kernel).
 int64_t arena_tiles(const acc_request &q) {
-  const int ipt = norm_ipt(tuned_ipt(q.kind, q.type, q.n), q.type);
+  const int ipt = ipt_for(q, BT);
   const int64_t ts = (int64_t)ipt * BT;
   const int64_t nt = (q.n + ts - 1) / ts;
   return (q.kind == ACC_REQ_FOLD && nt == 0) ? 1 : nt;
@@ -523,7 +581,7 @@ int arena_launch(BatchArena *ar, const acc_request *reqs, int64_t count, cudaStr
   int64_t nitems = 0;
   for (int64_t i = 0; i < count; ++i) {
     const acc_request &q = reqs[i];
-    const int ipt = norm_ipt(tuned_ipt(q.kind, q.type, q.n), q.type);
+    const int ipt = ipt_for(q, BT);
     const int64_t ts = (int64_t)ipt * BT;
     int64_t nt = (q.n + ts - 1) / ts;
     if (q.kind == ACC_REQ_FOLD && nt == 0) nt = 1;
@@ -564,7 +622,7 @@ void arena_free(BatchArena *ar) {
 }
 
 // ---------------------------------------------------------------- autotune
-static int autotune_run(int kind, int type, int bucket, cudaStream_t s, void *buf, size_t buf_bytes, int *best) {
+static int autotune_run(int kind, int type, int bucket, cudaStream_t s, void *buf, size_t buf_bytes, TuneVal *best) {
   const int64_t n = int64_t(1) << bucket;
   const int eb = type_bytes(type);
   // A batch of equal requests of this bucket's size, up to 2^24 elements in all.
@@ -579,28 +637,31 @@ static int autotune_run(int kind, int type, int bucket, cudaStream_t s, void *bu
     q.out = base + (size_t)n * eb + (kind == ACC_REQ_SCAN ? (size_t)i * n * eb : (size_t)i * eb);
   }
   float best_ms = 1e30f;
-  int best_ipt = default_ipt(kind, type, n);
-  for (int ipt = 1; ipt <= max_ipt(type); ipt *= 2) {
-    std::vector<int32_t> ov(count, ipt);
-    Batch *b = nullptr;
-    int st = batch_make(ACC_ADD, reqs.data(), count, ov.data(), &b);
-    if (st) return st;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    batch_launch_raw(b, s);
-    cudaEventRecord(e0, s);
-    for (int rep = 0; rep < 3; ++rep) batch_launch_raw(b, s);
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    batch_free(b);
-    if (ms < best_ms) { best_ms = ms; best_ipt = ipt; }
+  TuneVal pick{default_ipt(kind, type, n), BT};
+  // every launch shape, and for each every tile shape
+  for (int nt : B_NT) {
+    for (int ipt = 1; ipt <= max_ipt(type, nt); ipt *= 2) {
+      std::vector<int32_t> ov(count, ipt);
+      Batch *b = nullptr;
+      int st = batch_make(ACC_ADD, reqs.data(), count, ov.data(), nt, &b);
+      if (st) return st;
+      cudaEvent_t e0, e1;
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      batch_launch_raw(b, s);
+      cudaEventRecord(e0, s);
+      for (int rep = 0; rep < 3; ++rep) batch_launch_raw(b, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      batch_free(b);
+      if (ms < best_ms) { best_ms = ms; pick = TuneVal{ipt, nt}; }
+    }
   }
-  *best = best_ipt;
+  *best = pick;
   return check_launch();
 }
 
@@ -611,7 +672,7 @@ using namespace accgb;
 extern "C" int acc_batch_create(int op, const acc_request *reqs, int64_t count, acc_batch **out) {
   if (!out) return ACC_ERR_INVALID;
   Batch *b = nullptr;
-  int st = batch_make(op, reqs, count, nullptr, &b);
+  int st = batch_make(op, reqs, count, nullptr, 0, &b);
   if (st) return st;
   *out = reinterpret_cast<acc_batch *>(b);
   return ACC_OK;
@@ -676,14 +737,14 @@ extern "C" int acc_batch_autotune(const char *table_path, void *stream) {
   cudaError_t e = cudaMalloc(&buf, buf_bytes);
   if (e != cudaSuccess) return cuda_status(e);
   cudaMemset(buf, 0, buf_bytes);
-  std::map<TuneKey, int> table;
+  std::map<TuneKey, TuneVal> table;
   const int kinds[2] = {ACC_REQ_FOLD, ACC_REQ_SCAN};
   const int types[4] = {ACC_I32, ACC_F32, ACC_I64, ACC_F64};
   int st = ACC_OK;
   for (int kind : kinds)
     for (int type : types)
       for (int bucket = 8; bucket <= 22 && st == ACC_OK; ++bucket) {
-        int best = 0;
+        TuneVal best{0, BT};
         st = autotune_run(kind, type, bucket, s, buf, buf_bytes, &best);
         if (st == ACC_OK) table[TuneKey{kind, type, bucket}] = best;
       }
@@ -698,10 +759,12 @@ extern "C" int acc_batch_autotune(const char *table_path, void *stream) {
     if (!f) return ACC_ERR_INVALID;
     cudaDeviceProp p;
     cudaGetDeviceProperties(&p, 0);
-    fprintf(f, "{\"gpu\": \"%s\", \"threads\": %d, \"entries\": [", p.name, BT);
+    // entries: [kind, type, log2 size bucket, elements per thread, threads per CTA]
+    fprintf(f, "{\"gpu\": \"%s\", \"entries\": [", p.name);
     bool first = true;
     for (auto &kv : table) {
-      fprintf(f, "%s[%d, %d, %d, %d]", first ? "" : ", ", kv.first.kind, kv.first.type, kv.first.bucket, kv.second);
+      fprintf(f, "%s[%d, %d, %d, %d, %d]", first ? "" : ", ", kv.first.kind, kv.first.type, kv.first.bucket,
+              kv.second.ipt, kv.second.nt);
       first = false;
     }
     fprintf(f, "]}\n");
@@ -721,11 +784,18 @@ extern "C" int acc_batch_load_tuning(const char *table_path) {
   fclose(f);
   const size_t at = text.find("\"entries\"");
   if (at == std::string::npos) return ACC_ERR_INVALID;
-  std::map<TuneKey, int> table;
+  // entries of five numbers, or of four (tables written before the launch
+  // shape was tuned: 256 threads per CTA)
+  std::map<TuneKey, TuneVal> table;
   const char *p = text.c_str() + at;
   while ((p = strchr(p, '[')) != nullptr) {
-    int kind, type, bucket, ipt;
-    if (sscanf(p, "[%d, %d, %d, %d]", &kind, &type, &bucket, &ipt) == 4) table[TuneKey{kind, type, bucket}] = ipt;
+    int kind, type, bucket, ipt, nt = BT;
+    const int got5 = sscanf(p, "[%d, %d, %d, %d, %d]", &kind, &type, &bucket, &ipt, &nt);
+    if (got5 >= 4) {
+      if (got5 == 4) nt = BT;
+      if (!valid_nt(nt)) return ACC_ERR_INVALID;
+      table[TuneKey{kind, type, bucket}] = TuneVal{ipt, nt};
+    }
     ++p;
   }
   std::lock_guard<std::mutex> lk(g_tune_mu);

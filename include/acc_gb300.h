@@ -386,10 +386,12 @@ typedef struct acc_request {
 
 typedef struct acc_batch acc_batch;  /* opaque plan */
 
-/* Plan a batch: validates the requests, cuts each into tiles whose size
- * comes from the autotuner table (acc_batch_autotune / acc_batch_load_tuning;
- * built-in defaults otherwise) and allocates every scratch array the launch
- * will need.  The requests' buffers must stay valid while the plan is used. */
+/* Plan a batch: validates the requests, picks the launch shape (threads per
+ * CTA) that the autotuner table prefers for most of the batch's bytes, cuts
+ * each request into tiles whose shape comes from the same table
+ * (acc_batch_autotune / acc_batch_load_tuning; built-in defaults otherwise:
+ * 256 threads) and allocates every scratch array the launch will need.  The
+ * requests' buffers must stay valid while the plan is used. */
 int acc_batch_create(int op, const acc_request *reqs, int64_t count,
                      acc_batch **out);
 
@@ -409,13 +411,16 @@ int acc_batch_status(acc_batch *batch, void *stream);
 int acc_batch_destroy(acc_batch *batch);
 
 /* Autotuner: for fold and scan, Int32 / Float32 / Int64 / Float64 and every
- * size bucket 2^8 .. 2^22, time one batched launch per candidate tile size
- * (256 x 1, 2, 4, ... elements) and keep the fastest; the table is used by
+ * size bucket 2^8 .. 2^22, time one batched launch per candidate launch shape
+ * (128, 256 or 512 threads per CTA) and tile shape (1, 2, 4, ... elements per
+ * thread, tiles up to 32 KiB) and keep the fastest pair; the table is used by
  * later acc_batch_create calls and written as JSON to `table_path` (NULL:
- * not written). */
+ * not written), one entry [kind, type, bucket, elements per thread, threads
+ * per CTA] per key. */
 int acc_batch_autotune(const char *table_path, void *stream);
 
-/* Load a table written by acc_batch_autotune. */
+/* Load a table written by acc_batch_autotune (entries of four numbers, without
+ * the threads per CTA, mean 256). */
 int acc_batch_load_tuning(const char *table_path);
 
 /* ---------------------------------------------------------------- serving */

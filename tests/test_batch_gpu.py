@@ -154,6 +154,42 @@ def test_batch_uses_a_loaded_tuning_table(acc, dev, tmp_path):
     b.close()
 
 
+@pytest.mark.parametrize("nt", [128, 512])
+@pytest.mark.parametrize("f", ["+", "max"])
+def test_batch_launch_shapes_from_the_table(acc, orc, dev, tmp_path, nt, f):
+    """A table whose entries choose 128 or 512 threads per CTA (and tiles of
+    the largest and smallest shapes for them): the batch launches with that
+    shape and every request matches the oracle."""
+    big = 32768 // (nt * 8)  # the largest elements per thread for 8-byte types
+    entries = [[k, t, bucket, big if bucket % 2 else 1, nt] for k in (0, 1) for t in (0, 1, 3, 4)
+               for bucket in range(0, 40)]
+    p = tmp_path / "tune.json"
+    p.write_text(json.dumps({"gpu": "test", "entries": entries}))
+    acc.batch_load_tuning(p)
+    try:
+        rng = case_rng("batch_nt", nt, f)
+        reqs = make_requests(dev, f, rng)
+        b = acc.Batch(f, reqs)
+        b.launch()
+        b.status()
+        torch.cuda.synchronize()
+        for kind, xs, out, z in reqs:
+            check(orc, out, kind, xs, z, f)
+        b.close()
+    finally:
+        # back to 256 threads for the tests that follow
+        reset = [[k, t, bucket, 8, 256] for k in (0, 1) for t in (0, 1, 3, 4) for bucket in range(0, 40)]
+        p.write_text(json.dumps({"gpu": "test", "entries": reset}))
+        acc.batch_load_tuning(p)
+
+
+def test_batch_rejects_a_bad_launch_shape_in_the_table(acc, tmp_path):
+    p = tmp_path / "tune.json"
+    p.write_text(json.dumps({"gpu": "test", "entries": [[0, 0, 10, 4, 300]]}))
+    with pytest.raises(acc.AccError):
+        acc.batch_load_tuning(p)
+
+
 def test_batch_rejects_bad_requests(acc, dev):
     e = torch.empty(0, dtype=torch.int32, device=dev)
     with pytest.raises(acc.AccError) as err:

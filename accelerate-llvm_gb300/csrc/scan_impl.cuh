@@ -67,6 +67,7 @@ struct ScanArgs {
   int zop;           // ... MAP kernels: it is zop(in[i], c)
   uint64_t mapc;     // MAP kernels: the constant c (bits of one element)
   int64_t seg_len;   // segmented (row) scans: the rows' length; a row restarts the scan
+  void *seg_sums;    // ... with a seed (scanl' / scanr'): each row's total, or null
 };
 
 __device__ __forceinline__ int swz(int row, int chunk) { return row * SCAN_ROW_BYTES + ((chunk ^ (row & 7)) << 4); }
@@ -497,14 +498,17 @@ __device__ __forceinline__ void zip_row(unsigned char *buf, const unsigned char 
 // see segmented combinations.  A tile that holds a row start publishes its
 // last row's partial sum as an inclusive prefix at once (its successors need
 // nothing before it), and a tile that begins with a row start needs no
-// look-back.
+// look-back.  SEG 2 (scanl' / scanr' over rows: exclusive, each row's total
+// to seg_sums): every row restarts from the seed, and the thread whose line
+// holds a row's last element in scan order writes the row's total; SEG 1
+// (scanl1 / scanr1) carries none of that.
 constexpr int L2S_COMPUTE = SCAN_THREADS;
 constexpr int L2S_THREADS = L2S_COMPUTE + 32;
 constexpr int L2S_TILE = SCAN_THREADS * SCAN_ROW_BYTES;
 constexpr int L2S_CTAS_PER_SM = 3;
 constexpr bool L2S_HINTS = true;  // L2 policies: keep a tile between its two loads, drop it after
 
-template <int OP, class T, int PREC, bool R2L, int PROD = 0, bool SEG = false>
+template <int OP, class T, int PREC, bool R2L, int PROD = 0, int SEG = 0>
 __global__ void __launch_bounds__(L2S_THREADS, PROD == 2 ? 2 : L2S_CTAS_PER_SM)
 scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ CUtensorMap tout, ScanArgs a,
                const __grid_constant__ CUtensorMap tin2) {
@@ -632,7 +636,19 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     const int64_t jb = R2L ? a.seg_len - 1 - r0 : (r0 == 0 ? 0 : a.seg_len - r0);
     return jb < ITEMS ? (int)jb : ITEMS;
   };
+  // SEG: the offset of the last element in scan order of a row in tile t's
+  // line, or ITEMS
+  auto seg_end = [&](int64_t t) -> int {
+    const int64_t e0 = (t * SCAN_THREADS + tid) * (int64_t)ITEMS;
+    const int64_t r0 = e0 % a.seg_len;
+    const int64_t je = R2L ? (r0 == 0 ? 0 : a.seg_len - r0) : a.seg_len - 1 - r0;
+    return je < ITEMS ? (int)je : ITEMS;
+  };
+  // SEG: the state a row starts from
+  const S seg_reset = SEG == 2 ? A::lift(from_bits<T>(a.seed)) : A::id();
   (void)seg_start;
+  (void)seg_end;
+  (void)seg_reset;
   int64_t d_new = s_claim;
   int64_t t_cur = -1;
   S excl_cur = A::id();
@@ -683,13 +699,13 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         if (!R2L) {
 #pragma unroll
           for (int j = 0; j < ITEMS; ++j) {
-            if (j == jb) agg = A::id();
+            if (j == jb) agg = seg_reset;
             agg = A::push(agg, x[j]);
           }
         } else {
 #pragma unroll
           for (int j = ITEMS - 1; j >= 0; --j) {
-            if (j == jb) agg = A::id();
+            if (j == jb) agg = seg_reset;
             agg = A::push(agg, x[j]);
           }
         }
@@ -781,7 +797,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       S inner = A::id();
       const S pfx = s_prefix[pc];
       S run;
-      int jb = ITEMS;
+      int jb = ITEMS, je = ITEMS;
       if constexpr (SEG) {
         bool f = false;
         if (!R2L) {
@@ -792,6 +808,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         inner = seg_then(f, inner, exf_cur, excl_cur, f);
         run = f ? inner : (R2L ? A::comb(inner, pfx) : A::comb(pfx, inner));
         jb = seg_start(t_cur);
+        if constexpr (SEG == 2) je = seg_end(t_cur);
       } else {
         if (!R2L) {
           for (int w = 0; w < warp; ++w) inner = A::comb(inner, s_warp[pc][w]);
@@ -813,9 +830,10 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
         for (int kk = 0; kk < VEC; ++kk) {
           const int q = R2L ? VEC - 1 - kk : kk;
           const int j = c * VEC + q;
-          if (SEG && j == jb) run = A::id();
+          if (SEG && j == jb) run = seg_reset;
           if (a.exclusive) { y[q] = A::lower(run); run = A::push(run, x[j]); }
           else { run = A::push(run, x[j]); y[q] = A::lower(run); }
+          if (SEG == 2 && j == je) static_cast<T *>(a.seg_sums)[(e0 + j) / a.seg_len] = A::lower(run);
         }
         if (in_smem) {
           uint4 v;
@@ -1079,10 +1097,10 @@ int launch_scan_1d_sub(Workspace *w, const T *in, T *out, T *total_out, T *seed_
 
 // The persistent L2-re-read kernel; *launched false when the array cannot be
 // described by a TMA tensor map or the cooperative grid cannot be placed.
-template <int OP, class T, int PREC, bool R2L, int PROD = 0, bool SEG = false>
+template <int OP, class T, int PREC, bool R2L, int PROD = 0, int SEG = 0>
 int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n, bool has_seed,
                    bool exclusive, uint64_t seed, cudaStream_t s, bool *launched, const T *in2 = nullptr,
-                   int zop = 0, uint64_t mapc = 0, int64_t seg_len = 0) {
+                   int zop = 0, uint64_t mapc = 0, int64_t seg_len = 0, T *seg_sums = nullptr) {
   constexpr int ITEMS = SCAN_ROW_BYTES / sizeof(T);
   *launched = false;
   CUtensorMap tin, tout, tin2;
@@ -1128,6 +1146,7 @@ int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   a.zop = zop;
   a.mapc = mapc;
   a.seg_len = SEG ? seg_len : 1;
+  a.seg_sums = SEG ? seg_sums : nullptr;
   int64_t grid = (int64_t)device_info().sms * per_sm;
   if (grid > ntiles) grid = ntiles;
   // A cooperative launch places every CTA at once (or fails): the tiles a CTA
@@ -1147,10 +1166,11 @@ int launch_scan_l2(Workspace *w, const T *in, T *out, T *total_out, T *seed_out,
   return cuda_status(e);
 }
 
-// Tile size: 2 sub-tiles (64 KiB, 3 CTAs per SM) by default, the faster of
-// the two on GB300 at 2^25..2^28 elements; ACC_GB300_SCAN_SUB=1 selects 32 KiB
-// tiles (6 CTAs per SM).  A scan over a fused map (MAP: map (\x -> mop x c))
-// always takes the 64 KiB tiles.
+// Large arrays take the persistent kernel (over a fused map as well).  The
+// tile kernel's size below that: 2 sub-tiles (64 KiB, 3 CTAs per SM) by
+// default, the faster of the two on GB300 at 2^25..2^28 elements;
+// ACC_GB300_SCAN_SUB=1 selects 32 KiB tiles (6 CTAs per SM).  A scan over a
+// fused map (MAP: map (\x -> mop x c)) always takes the 64 KiB tiles there.
 template <int OP, class T, int PREC, bool R2L, bool MAP = false>
 int launch_scan_1d(Workspace *w, const T *in, T *out, T *total_out, T *seed_out, int64_t n,
                    bool has_seed, bool exclusive, uint64_t seed, cudaStream_t s, int mop = 0,
@@ -1303,13 +1323,14 @@ int launch_scan_zip_1d(Workspace *w, const T *in, const T *in2, int zop, T *out,
   return check_launch();
 }
 
-// scanl1 / scanr1 over the rows of a contiguous [outer x inner] array by the
+// scanl1 / scanr1 (and scanl' / scanr' with their row totals: primed) over
+// the rows of a contiguous [outer x inner] array by the
 // persistent kernel's segmented form (scan_seg.cu, a translation unit of its
 // own); *launched false where it does not apply (operator outside + * min
 // max, rows shorter than a 128-byte line, the array not describable by a TMA
 // tensor map), and the row kernels take the call.
-int scan_rows_seg(Workspace *w, int op, int type, int prec, bool r2l, const void *in, void *out, int64_t outer,
-                  int64_t inner, cudaStream_t s, bool *launched);
+int scan_rows_seg(Workspace *w, int op, int type, int prec, bool r2l, const void *in, void *out, void *sums,
+                  bool primed, uint64_t seed, int64_t outer, int64_t inner, cudaStream_t s, bool *launched);
 template <class T> constexpr int type_code() {
   return std::is_same<T, int32_t>::value ? ACC_I32 : std::is_same<T, int64_t>::value ? ACC_I64
        : std::is_same<T, uint32_t>::value ? ACC_U32 : std::is_same<T, float>::value ? ACC_F32 : ACC_F64;
@@ -1357,12 +1378,15 @@ int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, in
     }
   }
   if constexpr (!ZIP && !MAP) {
-    // Long scanl1 / scanr1 over rows: one segmented pass over the whole array
-    // (at least four 32 KiB tiles per SM).
-    if (kind == ACC_SCAN_INCLUSIVE && outer * inner * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
+    // Long scanl1 / scanr1 / scanl' / scanr' over rows: one segmented pass
+    // over the whole array (at least four 32 KiB tiles per SM).
+    if ((kind == ACC_SCAN_INCLUSIVE || kind == ACC_SCAN_PRIME) &&
+        outer * inner * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
       bool launched = false;
       const int pc = PREC == 1 ? ACC_PREC_COMPENSATED : (PREC == 2 ? ACC_PREC_FP64ACC : ACC_PREC_PLAIN);
-      const int st = scan_rows_seg(w, OP, type_code<T>(), pc, r2l, in, out, outer, inner, s, &launched);
+      const bool primed = kind == ACC_SCAN_PRIME;
+      const int st = scan_rows_seg(w, OP, type_code<T>(), pc, r2l, in, out, primed ? sums : nullptr, primed, seed,
+                                   outer, inner, s, &launched);
       if (st || launched) return st;
     }
   }

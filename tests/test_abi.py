@@ -132,6 +132,22 @@ def test_argument_validation_without_device(lib):
     assert lib.acc_selftest_timeout(7, N) == 1                                    # no such wait
 
 
+def test_batch_tuning_table_loader(lib, tmp_path):
+    """The autotuner table's loader (no device work): entries of five numbers
+    (elements per thread, threads per CTA) or four (256 threads); a launch
+    shape other than 128 / 256 / 512 threads, a file without entries or no
+    file are rejected."""
+    p = tmp_path / "tune.json"
+    p.write_text('{"gpu": "x", "entries": [[0, 0, 10, 4, 128], [1, 3, 12, 8, 512], [1, 4, 9, 2]]}')
+    assert lib.acc_batch_load_tuning(str(p).encode()) == 0
+    p.write_text('{"gpu": "x", "entries": [[0, 0, 10, 4, 300]]}')
+    assert lib.acc_batch_load_tuning(str(p).encode()) == 1
+    p.write_text('{"gpu": "x"}')
+    assert lib.acc_batch_load_tuning(str(p).encode()) == 1
+    assert lib.acc_batch_load_tuning(str(tmp_path / "missing.json").encode()) == 1
+    assert lib.acc_batch_load_tuning(None) == 1
+
+
 def test_c_caller_links_and_validates(lib, tmp_path):
     """The header compiles as strict C99 and a C program linked against the
     library by name gets the same answers as the ctypes calls above (a

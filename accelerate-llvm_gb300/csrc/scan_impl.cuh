@@ -500,7 +500,11 @@ __device__ __forceinline__ void zip_row(unsigned char *buf, const unsigned char 
 // nothing before it), and a tile that begins with a row start needs no
 // look-back.  SEG 2 (scanl' / scanr' over rows: exclusive, each row's total
 // to seg_sums): every row restarts from the seed, and the thread whose line
-// holds a row's last element in scan order writes the row's total; SEG 1
+// holds a row's last element in scan order writes the row's total; SEG 3
+// (scanl z / scanr z over rows, whose output rows are one element longer):
+// every row restarts from the seed and pass 2 stores each element straight to
+// its place in the longer output row (index + row), the row's total (scanl
+// z) or the seed (scanr z) going to the row's extra last slot; SEG 1
 // (scanl1 / scanr1) carries none of that.
 constexpr int L2S_COMPUTE = SCAN_THREADS;
 constexpr int L2S_THREADS = L2S_COMPUTE + 32;
@@ -645,7 +649,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
     return je < ITEMS ? (int)je : ITEMS;
   };
   // SEG: the state a row starts from
-  const S seg_reset = SEG == 2 ? A::lift(from_bits<T>(a.seed)) : A::id();
+  const S seg_reset = SEG >= 2 ? A::lift(from_bits<T>(a.seed)) : A::id();
   (void)seg_start;
   (void)seg_end;
   (void)seg_reset;
@@ -822,6 +826,16 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       const int64_t grow = t_cur * SCAN_THREADS + tid;
       const bool in_smem = grow < a.full_rows;
       const int64_t e0 = grow * ITEMS;
+      // SEG 3: element e0 + j goes to index e0 + j + (its row).  jlast: the
+      // offset of the last element of the first element's row, if the line
+      // holds it (-1 otherwise); the elements after it lie in the next row.
+      int64_t orow = 0;
+      int jlast = -1;
+      if constexpr (SEG == 3) {
+        orow = e0 / a.seg_len;
+        const int64_t left = a.seg_len - (e0 - orow * a.seg_len);  // elements of the row from e0 on
+        jlast = left <= ITEMS ? (int)(left - 1) : -1;
+      }
 #pragma unroll
       for (int cc = 0; cc < ITEMS / VEC; ++cc) {
         const int c = R2L ? ITEMS / VEC - 1 - cc : cc;
@@ -834,7 +848,17 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
           if (a.exclusive) { y[q] = A::lower(run); run = A::push(run, x[j]); }
           else { run = A::push(run, x[j]); y[q] = A::lower(run); }
           if (SEG == 2 && j == je) static_cast<T *>(a.seg_sums)[(e0 + j) / a.seg_len] = A::lower(run);
+          if constexpr (SEG == 3) {
+            if (e0 + j < a.n) {
+              const int64_t o = e0 + j + orow + ((jlast >= 0 && j > jlast) ? 1 : 0);
+              dst[o] = y[q];
+              // the row's extra slot follows its last element in memory:
+              // the total for scanl z, the seed for scanr z
+              if (j == jlast) dst[o + 1] = R2L ? from_bits<T>(a.seed) : A::lower(run);
+            }
+          }
         }
+        if constexpr (SEG == 3) continue;  // stored above, not through shared memory
         if (in_smem) {
           uint4 v;
           memcpy(&v, y, 16);
@@ -847,7 +871,7 @@ scan_l2_kernel(const __grid_constant__ CUtensorMap tin, const __grid_constant__ 
       }
       fence_proxy_async_smem();
       named_bar_sync<1, L2S_COMPUTE>();
-      if (tid == 0) {
+      if (tid == 0 && SEG != 3) {
         if constexpr (L2S_HINTS) tma_store_2d_hint(&tout, 0, (int)(t_cur * SCAN_THREADS), bufB, l2_policy_evict_first());
         else tma_store_2d(&tout, 0, (int)(t_cur * SCAN_THREADS), bufB);
         tma_store_commit();
@@ -1323,14 +1347,14 @@ int launch_scan_zip_1d(Workspace *w, const T *in, const T *in2, int zop, T *out,
   return check_launch();
 }
 
-// scanl1 / scanr1 (and scanl' / scanr' with their row totals: primed) over
-// the rows of a contiguous [outer x inner] array by the
+// Every scan flavour (kind: ACC_SCAN_INCLUSIVE / SEEDED / PRIME) over the
+// rows of a contiguous [outer x inner] array by the
 // persistent kernel's segmented form (scan_seg.cu, a translation unit of its
 // own); *launched false where it does not apply (operator outside + * min
 // max, rows shorter than a 128-byte line, the array not describable by a TMA
 // tensor map), and the row kernels take the call.
-int scan_rows_seg(Workspace *w, int op, int type, int prec, bool r2l, const void *in, void *out, void *sums,
-                  bool primed, uint64_t seed, int64_t outer, int64_t inner, cudaStream_t s, bool *launched);
+int scan_rows_seg(Workspace *w, int op, int type, int prec, bool r2l, int kind, const void *in, void *out,
+                  void *sums, uint64_t seed, int64_t outer, int64_t inner, cudaStream_t s, bool *launched);
 template <class T> constexpr int type_code() {
   return std::is_same<T, int32_t>::value ? ACC_I32 : std::is_same<T, int64_t>::value ? ACC_I64
        : std::is_same<T, uint32_t>::value ? ACC_U32 : std::is_same<T, float>::value ? ACC_F32 : ACC_F64;
@@ -1380,13 +1404,11 @@ int scan_typed(Workspace *w, int dir, int kind, const T *in, T *out, T *sums, in
   if constexpr (!ZIP && !MAP) {
     // Long scanl1 / scanr1 / scanl' / scanr' over rows: one segmented pass
     // over the whole array (at least four 32 KiB tiles per SM).
-    if ((kind == ACC_SCAN_INCLUSIVE || kind == ACC_SCAN_PRIME) &&
-        outer * inner * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
+    if (outer * inner * (int64_t)sizeof(T) >= (int64_t)device_info().sms * 4 * L2S_TILE) {
       bool launched = false;
       const int pc = PREC == 1 ? ACC_PREC_COMPENSATED : (PREC == 2 ? ACC_PREC_FP64ACC : ACC_PREC_PLAIN);
-      const bool primed = kind == ACC_SCAN_PRIME;
-      const int st = scan_rows_seg(w, OP, type_code<T>(), pc, r2l, in, out, primed ? sums : nullptr, primed, seed,
-                                   outer, inner, s, &launched);
+      const int st = scan_rows_seg(w, OP, type_code<T>(), pc, r2l, kind, in, out, kind == ACC_SCAN_PRIME ? sums : nullptr,
+                                   seed, outer, inner, s, &launched);
       if (st || launched) return st;
     }
   }

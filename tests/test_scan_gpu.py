@@ -117,11 +117,10 @@ def test_scan_many_short_rows(acc, orc, dev, t, op, shape):
                                         ("f32", "+", (1000, 5003)), ("f64", "min", (4097, 1000)),
                                         ("i32", "*", (2000, 4099)), ("u32", "max", (3, 2_000_003))])
 def test_scan_rows_segmented(acc, orc, dev, t, op, shape):
-    # scanl1 / scanr1, and scanl' / scanr' (every row from the seed, the row
-    # totals in a second array)
-    for d in (0, 1):
-        for k in (0, 2):
-            run_scan(acc, orc, dev, t, op, shape, d, k)
+    # scanl1 / scanr1, scanl z / scanr z (every row from the seed, output rows
+    # one element longer) and scanl' / scanr' (the row totals in a second array)
+    for d, k in FLAVOURS:
+        run_scan(acc, orc, dev, t, op, shape, d, k)
 
 
 @pytest.mark.parametrize("offset", [1, 3])

@@ -1,6 +1,6 @@
 """oracle -- numpy front end of liboracle.so (the C restatement in oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the checker of tests/ and __graft_entry__.smoke(),
+TEST INFRASTRUCTURE ONLY: the oracle of tests/ and __graft_entry__.smoke(),
 and the timed CPU baseline of bench.py.  The product path never imports it.
 
 Every function takes and returns numpy arrays and mirrors one entry point of

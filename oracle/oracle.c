@@ -1,10 +1,10 @@
 /*
  * oracle.c -- CPU restatement of accelerate-llvm-native's skeleton semantics.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library
- * (tests/, __graft_entry__.smoke()) and the timed CPU baseline of bench.py
- * (its `cpu_baseline` leg and `--impl reference`).  Nothing in the product
- * path links, loads or calls it.
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU library's
+ * results are compared with (tests/, __graft_entry__.smoke()) and the timed
+ * CPU baseline of bench.py (its `cpu_baseline` leg and `--impl reference`).
+ * Nothing in the product path links, loads or calls it.
  *
  * The reference CPU backend (accelerate-llvm-native) is Haskell that emits
  * LLVM IR at run time; it cannot be built here (no GHC, no clang, and the

@@ -1,4 +1,4 @@
-"""Shared fixtures: the skeleton library (CUDA), the oracle (CPU checker)."""
+"""Shared fixtures: the skeleton library (CUDA), the oracle (CPU restatement)."""
 import pathlib
 import sys
 
